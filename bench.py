@@ -1,0 +1,342 @@
+"""Benchmark of the per-timestep update on the 2-D shock-bubble workload.
+
+Workload: water (stiffened gas, gamma 4.4, p_inf 6e8) with a Mach-1.5 shock
+hitting an air bubble (radius 0.2, seeded centre), 1024 x 1024 cells,
+max_grid_size 128 (64 boxes), MUSCL + BVD-THINC (beta 1.6), CFL 0.4. One
+"step" is one full iteration of the reference's time loop (CFL reduction,
+two RK stages, RK2 average, cleanUpAlpha) over all cells.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--precision mixed|fp64]
+    python bench.py --impl reference ...   # the CPU reference arm
+
+Prints one JSON line. `value` is cell-updates/s over the K timed steps
+(device time, CUDA events on the library's stream, inputs resident in HBM);
+`e2e` is the same metric through the C ABI with the state copied in from
+pinned host memory and back out every step. Under torchrun each rank runs an
+independent replica (the update does not shard across GPUs in this build).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_CELLS = 1024
+MAX_GRID = 128
+METRIC = "cell-updates/s/GPU (FP32 vs FP64 at stated L1 err); adjoint/forward time ratio"
+WORKLOAD = "2-D shock-bubble interface, water/air, 1024x1024, MUSCL+THINC beta 1.6, CFL 0.4, max_grid_size 128"
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.file = None
+
+    def __enter__(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.file, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.file:
+            return None
+        try:
+            rows = [l.strip().split(",") for l in open(self.file.name) if l.strip()]
+        except Exception:
+            return None
+        finally:
+            try:
+                os.unlink(self.file.name)
+            except Exception:
+                pass
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                smax.append(float(r[2]))
+                for n, v in zip(names, r[5:9]):
+                    if v.strip().lower() in ("active", "1", "yes"):
+                        reasons.add(n)
+            except Exception:
+                continue
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def l2_flush_bytes():
+    return 256 << 20  # larger than the 129 MB L2
+
+
+def run_gpu_arm(args):
+    import torch
+
+    from tenjin_gb300 import build, cases
+    from tenjin_gb300.host import FP64, MIXED, TenjinGPU
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    build.build()
+    precision = MIXED if args.precision == "mixed" else FP64
+    case = cases.shock_bubble_2d(n=N_CELLS, max_grid_size=MAX_GRID, max_steps=1 << 30)
+    ncell = case.total_cells
+    g = TenjinGPU(case, precision)
+    lib = g.L
+    sp = ctypes.c_void_p()
+    lib.tj_get_stream(g.h, ctypes.byref(sp))
+    stream = torch.cuda.ExternalStream(sp.value)
+
+    # warm-up steps (untimed)
+    g.run(args.warmup, 1e300)
+    lib.tj_set_profiling(g.h, 1)
+    g.run(1, 1e300)  # capture with profiling, then reset totals
+    lib.tj_set_profiling(g.h, 0)
+    lib.tj_set_profiling(g.h, 1)
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    barrier()
+    torch.cuda.synchronize()
+    l0 = g.launch_count()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        with torch.cuda.stream(stream):
+            ev0.record(stream)
+        done, _ = g.run(args.steps, 1e300)
+        with torch.cuda.stream(stream):
+            ev1.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    ms = ev0.elapsed_time(ev1)
+    launches = g.launch_count() - l0
+    if ws > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    clocks = clk.summary()
+
+    # dominant kernel: per-launch time from the CUDA events around each launch
+    kernels = ["tj_stage_mixed", "tj_cfl_mixed"] if precision == MIXED else \
+        ["tj_recon_fp64", "tj_flux_fp64", "tj_update_fp64", "tj_cfl_fp64"]
+    ktimes = {}
+    for k in kernels:
+        tot, cnt = ctypes.c_double(), ctypes.c_longlong()
+        lib.tj_kernel_time(g.h, k.encode(), ctypes.byref(tot), ctypes.byref(cnt))
+        if cnt.value:
+            ktimes[k] = (tot.value, cnt.value)
+    lib.tj_set_profiling(g.h, 0)
+    dom = max(ktimes, key=lambda k: ktimes[k][0]) if ktimes else None
+    peaks, peak_src = measured_peaks()
+    roofline = None
+    if dom:
+        tot, cnt = ktimes[dom]
+        per_launch_s = tot / cnt / 1e3
+        if precision == MIXED:
+            # algorithmic bytes of one stage launch: the carried state (12 words
+            # of 4 B) read and written once; stage 2 also reads U^n: 5 state
+            # passes per step spread over 2 launches
+            bytes_per_launch = 2.5 * 12 * 4 * ncell
+        else:
+            bytes_per_launch = {"tj_recon_fp64": (7 + 2 * 14) * 8, "tj_flux_fp64": (2 * 14 + 9) * 8,
+                                "tj_update_fp64": (2 * 9 + 2 * 15) * 8, "tj_cfl_fp64": 10 * 8}[dom] * ncell
+        achieved = bytes_per_launch / per_launch_s / 1e9
+        traffic = None
+        try:
+            with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+                tj = json.load(f)
+            if tj.get("kernel") == dom:
+                traffic = tj.get("dram_bytes_per_launch")
+        except Exception:
+            pass
+        roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                    "frac": round(achieved / peaks["hbm_gbs"], 4), "traffic": traffic, "kernel": dom,
+                    "peak_source": peak_src, "launch_ms": round(tot / cnt, 4),
+                    "kernel_ms": {k: round(v[0] / v[1], 4) for k, v in ktimes.items()}}
+
+    # end to end through the C ABI: state in from pinned host memory, step,
+    # state out, every step
+    e2e = None
+    if args.e2e_steps > 0:
+        nc = g.ncomp
+        host = torch.empty((nc, 1, N_CELLS, N_CELLS), dtype=torch.float64, pin_memory=True)
+        host_np = host.numpy()
+        lib.tj_download_domain(g.h, 0, host_np.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+        for _ in range(args.e2e_steps):
+            p = host_np.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+            lib.tj_upload_domain(g.h, 0, p)
+            lib.tj_step(g.h, ctypes.c_double(1e300))
+            lib.tj_download_domain(g.h, 0, p)
+        with torch.cuda.stream(stream):
+            e1.record(stream)
+        torch.cuda.synchronize()
+        e2e_ms = e0.elapsed_time(e1)
+        wall = time.perf_counter() - t0
+        nbytes = nc * ncell * 8
+        e2e = {"value": ncell * args.e2e_steps / (max(e2e_ms / 1e3, wall)), "unit": "cell-updates/s",
+               "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes, "steps": args.e2e_steps,
+               "path": "tj_upload_domain + tj_step + tj_download_domain (AccessPattern layout, pinned host)"}
+
+    g.close()
+    value = ncell * args.steps * ws / (ms / 1e3)
+    line = {
+        "metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 (f64 closures)" if precision == MIXED else "f64",
+        "data": "synthetic (seeded shock-bubble initial condition)",
+        "config": {"workload": WORKLOAD, "cells": ncell, "precision": args.precision,
+                   "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
+                   "l2": "state working set larger than L2 (three state buffers of >= 48 MB plus scratch per step)"},
+        "gpu_launches": launches, "steps_done": done, "e2e": e2e, "roofline": roofline, "clocks": clocks,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def cpu_baseline(target_seconds=15.0):
+    """The oracle port (oracle/port, FP64, OpenMP over all host threads) on a
+    bounded sample of the same workload: the full 1024^2 domain for as many
+    steps as fit in about target_seconds."""
+    from oracle import port
+    from tenjin_gb300 import cases
+
+    port.build_port()
+    case = cases.shock_bubble_2d(n=N_CELLS, max_grid_size=MAX_GRID, max_steps=1)
+    sim = port.PortSim(case, omp=True)
+    t0 = time.perf_counter()
+    sim.run(max_steps=1)
+    one = time.perf_counter() - t0
+    steps = max(1, min(50, int(target_seconds / max(one, 1e-3))))
+    t0 = time.perf_counter()
+    sim.run(max_steps=steps)
+    el = time.perf_counter() - t0
+    return {"value": case.total_cells * steps / el, "unit": "cell-updates/s", "cores": port.threads(),
+            "kind": "port", "sample": f"{steps} steps of the 1024x1024 workload after 1 untimed step, FP64"}
+
+
+def run_reference_arm(args):
+    """CPU reference arm: the oracle port (the reference itself cannot be built
+    on the GPU host: it needs AMReX and its sources are not shipped there),
+    with all host threads, on the same workload and metric; each step is one
+    full time step of a bounded square sample of the domain."""
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle import port
+    from tenjin_gb300 import cases
+
+    port.build_port()
+    nthr = port.threads()
+    # size the sample so that (warmup + steps) stays within about two minutes
+    budget = 120.0 / max(1, args.steps + args.warmup)
+    n = 256
+    probe = cases.shock_bubble_2d(n=n, max_grid_size=MAX_GRID // 4, max_steps=1)
+    sim = port.PortSim(probe, omp=True)
+    t0 = time.perf_counter()
+    sim.run(max_steps=1)
+    rate = n * n / (time.perf_counter() - t0)
+    side = int((budget * rate) ** 0.5) // 64 * 64
+    side = max(64, min(N_CELLS, side))
+    mgs = max(16, MAX_GRID * side // N_CELLS)
+    case = cases.shock_bubble_2d(n=side, max_grid_size=mgs, max_steps=1 << 30)
+    sim = port.PortSim(case, omp=True)
+    sim.run(max_steps=args.warmup)
+    t0 = time.perf_counter()
+    sim.run(max_steps=args.steps)
+    el = time.perf_counter() - t0
+    value = case.total_cells * args.steps / el
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded shock-bubble initial condition)",
+        "config": {"workload": WORKLOAD, "sample": f"{side}x{side} cells (max_grid_size {mgs})"},
+        "cpu_baseline": {"value": value, "unit": "cell-updates/s", "cores": nthr, "kind": "port",
+                         "sample": f"{args.steps} steps of a {side}x{side} sample of the workload"},
+        "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["mixed", "fp64"])
+    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference_arm(args)
+    else:
+        run_gpu_arm(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,170 @@
+/* tenjin_gpu.h -- C ABI of the GB300 implementation of Tenjin's per-timestep
+ * update (libtenjin_gpu.so).
+ *
+ * The reference has no plugin or FFI layer: its operator surface is a set of
+ * C++ free functions and class methods called from the time loop
+ * (main.cpp:121-191). Each entry point below replaces one of them, working on
+ * state held in device memory by a context. The host exchanges state in the
+ * reference's own layout: one AMReX FArrayBox per box, components in
+ * AccessPattern order (accesspattern.cpp:44-79), component-major SoA with i
+ * fastest (Array4(i,j,k,n)), over the box grown by ngrow cells.
+ *
+ * Conventions
+ *   - Every call returns TJ_OK (0) or a negative TJ_ERR_* status; the
+ *     reference prints and calls exit(1) instead (e.g. hllc.cpp:199,
+ *     boxaccesscellarray.cpp:561,587). tj_last_error() gives the message.
+ *   - A context owns its device memory. Host buffers are read or written only
+ *     during the call. Work is ordered on the context's CUDA stream; calls
+ *     that return data to the host synchronise it. A context is not thread
+ *     safe: use one per host thread.
+ *   - All arithmetic of TJ_PRECISION_FP64 is IEEE binary64 in the
+ *     reference's evaluation order.
+ */
+#ifndef TENJIN_GPU_H
+#define TENJIN_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TJ_MAX_MATERIALS 4
+#define TJ_MAX_EOS_PARAMS 16
+
+/* status codes */
+#define TJ_OK 0
+#define TJ_ERR_ARG -1        /* invalid argument or unsupported parameter combination */
+#define TJ_ERR_CUDA -2       /* a CUDA call failed */
+#define TJ_ERR_NAN -3        /* NaN in the state (main.cpp:183-187) */
+#define TJ_ERR_WAVESPEED -4  /* NaN wave speed in the 5-wave solver (hllc.cpp:169-200,367-373) */
+#define TJ_ERR_ALPHA -5      /* volume-fraction scaling error (boxaccesscellarray.cpp:553-588) */
+#define TJ_ERR_PLASTIC -6    /* plastic divide by zero (plastic.cpp:189-193) */
+#define TJ_ERR_STATE -7      /* call out of order (no domain, no state) */
+
+/* equation-of-state kinds; parameter vectors as getMaterialParameters builds
+ * them (initialise.cpp:125-235) */
+#define TJ_EOS_MIEGRUNEISEN 0 /* [gamma, pref, eref, CV]                         equationofstate.cpp:5-115 */
+#define TJ_EOS_ROMENSKII 1    /* [gamma, pref, eref, CV, rho0, K0, a, b, G0]     equationofstate.cpp:403-495 */
+#define TJ_EOS_WILKINS 2      /* [gamma, pref, eref, CV, rho0, e1..e5, G0]       equationofstate.cpp:502-596 */
+#define TJ_EOS_HUGONIOT 3     /* [gamma, pref, eref, CV, rho0, c0, s, G0]: linear us-up Hugoniot reference
+                                 curve with constant Gruneisen gamma; no reference counterpart */
+
+#define TJ_PHASE_SOLID 0 /* Material_type (structdefinitions.h:36-40) */
+#define TJ_PHASE_FLUID 1
+
+#define TJ_BC_TRANSMISSIVE 0 /* Boundary_type (structdefinitions.h:51-55): foextrap */
+#define TJ_BC_REFLECTIVE 1   /* reflect_even, reflect_odd for the normal velocity and momentum */
+
+#define TJ_PRECISION_FP64 0  /* every operation in binary64, reference order */
+#define TJ_PRECISION_MIXED 1 /* binary32 bulk; binary64 pressure closure, sound speed and
+                                conserved-state accumulation */
+
+typedef struct tj_material {
+    int phase;        /* TJ_PHASE_* */
+    int eos;          /* TJ_EOS_* */
+    int nparams;
+    double params[TJ_MAX_EOS_PARAMS];
+    double yield_stress; /* PlasticEOS::yieldStress (plastic.h:21), solids only */
+} tj_material;
+
+/* Mirrors ParameterStruct (structdefinitions.h:105-144) plus the boundary
+ * types of InitialStruct (structdefinitions.h:165-166). */
+typedef struct tj_params {
+    int dim;          /* AMREX_SPACEDIM: 1, 2 or 3 */
+    int n_materials;  /* numberOfMaterials */
+    int n_mixtures;   /* numberOfMixtures: must be 0 */
+    int SOLID, THINC, RADIAL, PLASTIC, REACTIVE, MUSCL; /* RADIAL, REACTIVE: must be 0 */
+    int nghost;       /* Nghost: must be >= 2 */
+    int lo_bc[3], hi_bc[3];
+    double CFL, THINCbeta;
+    int precision;    /* TJ_PRECISION_* */
+    tj_material materials[TJ_MAX_MATERIALS];
+} tj_params;
+
+typedef struct tj_ctx tj_ctx;
+
+/* Context lifetime. */
+int tj_create(const tj_params* params, tj_ctx** out);
+int tj_destroy(tj_ctx* ctx);
+int tj_last_error(const tj_ctx* ctx, char* buf, unsigned long len);
+/* AccessPattern size Ncomp (main.cpp:55). */
+int tj_ncomp(const tj_ctx* ctx);
+
+/* Geometry. A context holds one or more independent domains (each its own
+ * Geometry with its own physical boundaries); they share one dt. Domain d
+ * covers cells [0, n_cells[3d+k]) along axis k with physical length
+ * dim_l[3d+k]. Replaces the BoxArray / Geometry set-up of main.cpp:34-46.
+ * Reallocates the device state (zeroed). */
+int tj_set_domains(tj_ctx* ctx, int ndomains, const int* n_cells, const double* dim_l);
+/* Box list of one domain in MFIter order, lo/hi inclusive (6 ints per box).
+ * Defaults to one box per domain. The box list must tile the domain. It
+ * matters for BVD-THINC only (thinc.cpp:57-63 reads box ghost cells). */
+int tj_set_boxes(tj_ctx* ctx, int domain, int nbox, const int* lohi);
+/* max_grid_size chopping of a domain (BoxArray::maxSize, main.cpp:36). */
+int tj_set_max_grid_size(tj_ctx* ctx, int domain, int max_grid_size);
+int tj_num_boxes(const tj_ctx* ctx, int domain);
+int tj_get_box(const tj_ctx* ctx, int domain, int box, int* lohi);
+int tj_num_cells(const tj_ctx* ctx, long long* ncells);
+
+/* State exchange in the reference's FArrayBox layout (box grown by ngrow,
+ * ncomp must equal tj_ncomp). Upload reads the valid cells; download writes
+ * the valid cells (ghosts untouched). */
+int tj_upload_state(tj_ctx* ctx, int domain, int box, const double* fab, int ncomp, int ngrow);
+int tj_download_state(tj_ctx* ctx, int domain, int box, double* fab, int ncomp, int ngrow);
+/* Whole-domain exchange: ncomp blocks of nx*ny*nz doubles (valid cells, i
+ * fastest), AccessPattern order. */
+int tj_upload_domain(tj_ctx* ctx, int domain, const double* data);
+int tj_download_domain(tj_ctx* ctx, int domain, double* data);
+/* Initial condition from primitive fields (alpha[M], rho_k[M], u[3], p,
+ * V[9] if SOLID, epsilon[M] if PLASTIC; each nx*ny*nz doubles), then
+ * primitiveToConservative: the last step of setInitialConditions
+ * (initialise.cpp:111-123). */
+int tj_set_primitive(tj_ctx* ctx, int domain, const double* prim);
+
+/* Operators of the time loop. */
+/* TimeStep::getTimeStep (timestep.cpp:36-70): CFL * min over cells and
+ * directions of dx/(a+|u|), after the halo fill of main.cpp:124-126. */
+int tj_compute_dt(tj_ctx* ctx, double* dt);
+/* advance (hllc.cpp:699-707): two HLLCadvance stages and U1 = (U + U2)/2. */
+int tj_advance(tj_ctx* ctx, double dt);
+/* PlasticEOS::plasticUpdate (plastic.cpp:227-244), radial return. */
+int tj_plastic_update(tj_ctx* ctx, double dt);
+/* CellArray::cleanUpV (boxaccesscellarray.cpp:476-528). */
+int tj_cleanup_v(tj_ctx* ctx);
+/* CellArray::cleanUpAlpha (boxaccesscellarray.cpp:530-599). */
+int tj_cleanup_alpha(tj_ctx* ctx);
+/* CellArray::conservativeToPrimitive / primitiveToConservative
+ * (boxaccesscellarray.cpp:67-174), on every valid cell. */
+int tj_cons_to_prim(tj_ctx* ctx);
+int tj_prim_to_cons(tj_ctx* ctx);
+/* CellArray::contains_nan (cellarray.cpp:101-116): *flag = 1 if NaN. */
+int tj_contains_nan(tj_ctx* ctx, int* flag);
+
+/* One iteration of the time loop of main.cpp:121-191 with dt and t kept on
+ * the device: dt = getTimeStep, clamped to t_end, times 0.2 for the first
+ * five steps; advance; plasticUpdate (PLASTIC); cleanUpV (SOLID);
+ * cleanUpAlpha; NaN check. Does not synchronise. */
+int tj_step(tj_ctx* ctx, double t_end);
+/* Run up to nsteps iterations or until t >= t_end. Steps are issued in
+ * groups captured as CUDA graphs; the host polls t between groups. */
+int tj_run(tj_ctx* ctx, int nsteps, double t_end, int* steps_done, double* t_out);
+/* Simulated time, step count and last dt (synchronises). */
+int tj_get_time(tj_ctx* ctx, double* t, int* nsteps, double* last_dt);
+int tj_set_time(tj_ctx* ctx, double t, int nsteps);
+/* Device-side status word of the last steps (sticky; TJ_OK if clean). */
+int tj_status(tj_ctx* ctx);
+int tj_synchronize(tj_ctx* ctx);
+/* Number of this library's kernel launches issued by the context so far. */
+int tj_launch_count(const tj_ctx* ctx, long long* count);
+/* The cudaStream_t that orders all work of the context. */
+int tj_get_stream(tj_ctx* ctx, void** stream);
+/* Per-kernel timing: when on, CUDA events are recorded around every launch of
+ * this library's kernels (also inside captured graphs); tj_kernel_time
+ * returns the summed duration and launch count of one kernel name since
+ * profiling was switched on. */
+int tj_set_profiling(tj_ctx* ctx, int on);
+int tj_kernel_time(tj_ctx* ctx, const char* kernel, double* ms_total, long long* launches);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

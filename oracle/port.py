@@ -42,7 +42,8 @@ def build_port(force: bool = False) -> None:
     os.makedirs(BUILD_DIR, exist_ok=True)
     for omp in (False, True):
         out = lib_path(omp)
-        if not force and os.path.exists(out) and os.path.getmtime(out) >= os.path.getmtime(SRC):
+        deps = [SRC, os.path.join(HERE, "port", "tenjin_port.h"), os.path.join(HERE, "shims", "tj_libm.h")]
+        if not force and os.path.exists(out) and os.path.getmtime(out) >= max(os.path.getmtime(f) for f in deps):
             continue
         cmd = ["gcc", "-O2", "-std=c99", "-ffp-contract=off", "-fPIC", "-shared", SRC, "-o", out, "-lm"]
         if omp:

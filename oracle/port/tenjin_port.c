@@ -5,6 +5,7 @@
  * same machine; build with -ffp-contract=off.
  */
 #include "tenjin_port.h"
+#include "../shims/tj_libm.h"
 
 #include <math.h>
 #include <stdlib.h>
@@ -275,12 +276,12 @@ static double eos_e_cold(const tjp_sim* s, int m, const ecell* e)
         case 1: {
             double a = PRM(m, 6), K0 = PRM(m, 5), r0 = PRM(m, 4);
             x = e->rhok / r0;
-            return e->arho * (((K0 / (2.0 * r0 * a * a)) * (pow(x, a) - 1.0)) * (pow(x, a) - 1.0));
+            return e->arho * (((K0 / (2.0 * r0 * a * a)) * (tjm_pow(x, a) - 1.0)) * (tjm_pow(x, a) - 1.0));
         }
         case 2: {
             double r0 = PRM(m, 4);
             x = e->rhok / r0;
-            return e->arho * ((PRM(m, 5) + PRM(m, 6) * x * x + PRM(m, 7) * x + PRM(m, 8) / x - PRM(m, 9) * log(x)) / r0);
+            return e->arho * ((PRM(m, 5) + PRM(m, 6) * x * x + PRM(m, 7) * x + PRM(m, 8) / x - PRM(m, 9) * tjm_log(x)) / r0);
         }
         default: {
             double r0 = PRM(m, 4), c0 = PRM(m, 5), sl = PRM(m, 6);
@@ -299,7 +300,7 @@ static double eos_p_cold(const tjp_sim* s, int m, const ecell* e)
         case 1: {
             double a = PRM(m, 6), K0 = PRM(m, 5), r0 = PRM(m, 4);
             x = e->rhok / r0;
-            return (e->alpha / G) * ((K0 / a) * pow(x, a + 1.0) * (pow(x, a) - 1.0));
+            return (e->alpha / G) * ((K0 / a) * tjm_pow(x, a + 1.0) * (tjm_pow(x, a) - 1.0));
         }
         case 2: {
             double r0 = PRM(m, 4);
@@ -319,7 +320,7 @@ static double eos_G(const tjp_sim* s, int m, const ecell* e)
 {
     switch (s->p.eos[m]) {
         case 0: return 0.0 * e->alpha;
-        case 1: return PRM(m, 8) * pow((e->rhok / PRM(m, 4)), PRM(m, 7) + 1.0);
+        case 1: return PRM(m, 8) * tjm_pow((e->rhok / PRM(m, 4)), PRM(m, 7) + 1.0);
         case 2: return PRM(m, 10);
         default: return PRM(m, 7);
     }
@@ -331,7 +332,7 @@ static double eos_dGdrho(const tjp_sim* s, int m, const ecell* e)
         case 0: return 0.0 * e->alpha;
         case 1: {
             double b = PRM(m, 7), r0 = PRM(m, 4);
-            return PRM(m, 8) * (b + 1.0) * pow((e->rhok / r0), b) / r0;
+            return PRM(m, 8) * (b + 1.0) * tjm_pow((e->rhok / r0), b) / r0;
         }
         default: return 0.0;
     }
@@ -343,7 +344,7 @@ static double eos_dG2drho2(const tjp_sim* s, int m, const ecell* e)
         case 0: return 0.0 * e->alpha;
         case 1: {
             double b = PRM(m, 7), r0 = PRM(m, 4);
-            return PRM(m, 8) * (b + 1.0) * (b)*pow((e->rhok / r0), b - 1.0) / (r0 * r0);
+            return PRM(m, 8) * (b + 1.0) * (b)*tjm_pow((e->rhok / r0), b - 1.0) / (r0 * r0);
         }
         default: return 0.0;
     }
@@ -377,7 +378,7 @@ static double eos_c2(const tjp_sim* s, int m, const ecell* e)
         case 0: return e->p * (G + 1.0) / e->rhok - PRM(m, 1) / e->rhok; /* :61-64 */
         case 1: {
             double a = PRM(m, 6), K0 = PRM(m, 5), r0 = PRM(m, 4), x = e->rhok / r0;
-            double dpc = (K0 / (a * r0)) * pow(x, a) * ((2.0 * a + 1.0) * pow(x, a) - (a + 1.0));
+            double dpc = (K0 / (a * r0)) * tjm_pow(x, a) * ((2.0 * a + 1.0) * tjm_pow(x, a) - (a + 1.0));
             double dps = e->rhok * eos_dG2drho2(s, m, e) * e->hj2;
             return (e->p * (G + 1.0) - (eos_p_cold(s, m, e) + eos_p_shear(s, m, e)) * (G + 1.0)) / e->rhok + dpc + dps +
                    (4.0 / 3.0) * eos_G(s, m, e) / e->rhok;
@@ -949,8 +950,8 @@ static int stage(tjp_sim* s, pdom* D, double* U, double* U1, double dt)
                     if (mixed) {
                         double nvc = (s->p.dim == 2) ? youngs(s, D, U, m, i, j, k, d) : 1.0;
                         double beta = nvc * beta0 + 0.01;
-                        double coshB = cosh(beta), tanhB = tanh(beta);
-                        double B = exp(theta * beta * ((2.0 * Cc) - 1.0));
+                        double coshB = tjm_cosh(beta), tanhB = tjm_tanh(beta);
+                        double B = tjm_exp(theta * beta * ((2.0 * Cc) - 1.0));
                         double A = ((B / coshB) - 1.0) / tanhB;
                         D->urstar[(size_t)m * N + c] = mn + (mx / 2.0) * (1.0 + theta * ((tanhB + A) / (1.0 + A * tanhB)));
                         D->ulstar[(size_t)m * N + c] = mn + (mx / 2.0) * (1.0 + theta * A);
@@ -1153,7 +1154,7 @@ static void cleanup_v_cell(tjp_sim* s, double* X, long N, long c)
     for (int q = 0; q < 9; ++q) V[q] = AT(X, C->V + q, c);
     mmT(V, V, B);
     sqrtm3(B, Sq);
-    double norm = pow(det3(Sq), -1.0 / 3.0);
+    double norm = tjm_pow(det3(Sq), -1.0 / 3.0);
     for (int r = 0; r < 3; ++r)
         for (int q = 0; q < 3; ++q)
             AT(X, C->V + 3 * r + q, c) = ((Sq[3 * r + q] * norm * ts) + (double)(r == q) * (ta - ts)) / ta;

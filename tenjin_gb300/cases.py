@@ -268,3 +268,51 @@ def uneven_boxes_3d(nbox: int = 4096, seed: int = 0, lo: int = 8, hi: int = 64, 
         doms.append(Domain(nn, [k * dx for k in nn], [[0, 0, 0, nn[0] - 1, nn[1] - 1, nn[2] - 1]], prim))
     c.domains = doms
     return c
+
+
+# ---------------------------------------------------------------------------
+# Parity workload: 2-D solid/fluid mixture with plasticity (any solid EOS).
+# ---------------------------------------------------------------------------
+
+def solid_mixture_2d(eos: int = EOS_WILKINS, n: int = 20, max_steps: int = 8, seed: int = 1,
+                     max_grid_size: int = 8, yield_stress: float = 3e8) -> Case:
+    """Solid (left half) against an ideal gas (right half) with a shear
+    perturbation of V and a moving flyer region; exercises the 5-wave solver,
+    the Hencky closure, the radial return and cleanUpV."""
+    if eos == EOS_WILKINS:
+        K, r0 = 7.6e10, 2785.0
+        prm = [3.0, 0.0, 0.0, 1.0, r0, 0.0, K / 2.0, 0.0, 0.0, 0.0, 2.76e10]
+    elif eos == EOS_ROMENSKII:
+        prm = [3.0, 0.0, 0.0, 1.0, 8930.0, 1.37e11, 1.0, 3.0, 4.6e10]
+    else:
+        prm = [CU_GAMMA0 + 1.0, 0.0, 0.0, 1.0, CU_RHO0, CU_C0, CU_S, CU_G]
+    mats = [Material(PHASE_SOLID, eos, prm, yield_stress),
+            Material(PHASE_FLUID, EOS_MIEGRUNEISEN, [1.4, 0.0, 0.0, 1.0])]
+    c = Case(f"solid_mixture_2d_eos{eos}", 2, mats, solid=1, plastic=1, cfl=0.4, max_steps=max_steps)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    prim = np.zeros((c.nprim, 1, n, n))
+    a = np.full((n, n), 1 - 1e-6)
+    a[:, n // 2:] = 1e-6
+    prim[0, 0] = a
+    prim[1, 0] = 1 - a
+    prim[2, 0] = prm[4] * (1 + 0.01 * rng.standard_normal((n, n)))
+    prim[3, 0] = 1.2
+    prim[4, 0] = np.where(np.arange(n)[None, :] < n // 3, 300.0, 0.0)
+    prim[5, 0] = 50.0 * rng.standard_normal((n, n))
+    prim[7, 0] = 1e5 + 1e7 * rng.uniform(size=(n, n))
+    V = np.eye(3)[:, :, None, None] + 0.01 * rng.standard_normal((3, 3, n, n))
+    for r in range(3):
+        for q in range(3):
+            prim[8 + 3 * r + q, 0] = V[r, q]
+    nn = [n, n, 1]
+    c.domains = [Domain(nn, [0.01, 0.01, 1.0], max_size_boxes(nn, 2, max_grid_size), prim)]
+    return c
+
+
+def fluid_boxes_3d(n: int = 12, max_grid_size: int = 5, max_steps: int = 5, seed: int = 0) -> Case:
+    """One 3-D water/air domain split into several boxes (MUSCL only)."""
+    c = uneven_boxes_3d(nbox=1, lo=n, hi=n, max_steps=max_steps, seed=seed)
+    d = c.domains[0]
+    d.boxes = max_size_boxes(d.n_cells, 3, max_grid_size)
+    c.name = "fluid_boxes_3d"
+    return c

@@ -1,0 +1,857 @@
+// C ABI of libtenjin_gpu.so (include/tenjin_gpu.h): context management,
+// domain/box bookkeeping, state exchange in the reference's FArrayBox layout
+// and the time-loop operators, dispatched to the FP64 reference-faithful
+// kernels or to the mixed-precision fused kernels.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "tj_fp64.cuh"
+#include "tj_mixed.cuh"
+#include "tj_types.h"
+
+using namespace tj;
+
+namespace {
+
+// CUDA-event timing of every kernel launch. Pairs recorded while a graph is
+// captured belong to that graph and are read after each of its launches;
+// pairs recorded by direct launches are read at the next synchronisation.
+struct EventProf : Prof {
+    struct Pair {
+        std::string name;
+        cudaEvent_t a, b;
+    };
+    std::vector<Pair> pool;
+    size_t cursor = 0, graph_end = 0;
+    bool capturing = false;
+    std::vector<std::pair<std::string, double>> totals;
+    std::vector<std::pair<std::string, long long>> counts;
+
+    void reserve(size_t n)
+    {
+        while (pool.size() < n) {
+            Pair p;
+            cudaEventCreate(&p.a);
+            cudaEventCreate(&p.b);
+            pool.push_back(p);
+        }
+    }
+    void begin(const char* kernel, void* st) override
+    {
+        if (cursor >= pool.size()) {
+            if (capturing) return;  // pool is sized before capture
+            reserve(pool.size() + 256);
+        }
+        pool[cursor].name = kernel;
+        cudaEventRecord(pool[cursor].a, (cudaStream_t)st);
+    }
+    void end(const char* kernel, void* st) override
+    {
+        (void)kernel;
+        if (cursor >= pool.size()) return;
+        cudaEventRecord(pool[cursor].b, (cudaStream_t)st);
+        ++cursor;
+    }
+    void add(const std::string& n, double ms)
+    {
+        for (auto& t : totals)
+            if (t.first == n) { t.second += ms; for (auto& c : counts) if (c.first == n) c.second += 1; return; }
+        totals.push_back({n, ms});
+        counts.push_back({n, 1});
+    }
+    // Accumulate pairs [lo, hi) (the stream has been synchronised).
+    void collect(size_t lo, size_t hi)
+    {
+        for (size_t i = lo; i < hi && i < pool.size(); ++i) {
+            float ms = 0.f;
+            if (cudaEventElapsedTime(&ms, pool[i].a, pool[i].b) == cudaSuccess) add(pool[i].name, ms);
+        }
+    }
+    void collect_direct()
+    {
+        collect(graph_end, cursor);
+        cursor = graph_end;
+    }
+    ~EventProf() override
+    {
+        for (auto& p : pool) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
+    }
+};
+
+}  // namespace
+
+struct tj_ctx {
+    tj_params params;
+    DevParams P;
+    std::string err;
+    cudaStream_t stream = nullptr;
+    // geometry
+    std::vector<DevDomain> doms;
+    std::vector<std::vector<int>> boxes;  // per domain, 6 ints per box
+    long long ntot = 0, nftot[3] = {0, 0, 0};
+    bool geometry_dirty = true;
+    // device memory
+    DevDomain* d_doms = nullptr;
+    int* d_boxes = nullptr;
+    int* d_cell_box = nullptr;
+    DevScalars* d_scal = nullptr;
+    double *A = nullptr, *B = nullptr, *C = nullptr, *UL = nullptr, *UR = nullptr, *FX = nullptr;
+    double *ulstar = nullptr, *urstar = nullptr, *gstar[3] = {nullptr, nullptr, nullptr};
+    double* staging = nullptr;
+    size_t staging_bytes = 0;
+    MixedState mixed;
+    // graph-captured step groups
+    cudaGraphExec_t graph_exec = nullptr;
+    int graph_steps = 0;
+    long long launches = 0;
+    EventProf* prof = nullptr;
+    long long graph_launches = 0;
+};
+
+namespace {
+
+int fail(tj_ctx* c, int code, const std::string& msg)
+{
+    if (c) c->err = msg;
+    return code;
+}
+
+#define TJ_CUDA(c, call)                                                                      \
+    do {                                                                                      \
+        cudaError_t e_ = (call);                                                              \
+        if (e_ != cudaSuccess) return fail((c), TJ_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+void make_layouts(const tj_params& p, DevParams& P)
+{
+    std::memset(&P, 0, sizeof P);
+    P.dim = p.dim;
+    P.M = p.n_materials;
+    P.solid = p.SOLID;
+    P.thinc = p.THINC;
+    P.plastic = p.PLASTIC;
+    P.muscl = p.MUSCL;
+    for (int d = 0; d < 3; ++d) { P.lo_bc[d] = p.lo_bc[d]; P.hi_bc[d] = p.hi_bc[d]; }
+    P.cfl = p.CFL;
+    P.beta = p.THINCbeta;
+    for (int m = 0; m < P.M; ++m) {
+        P.phase[m] = p.materials[m].phase;
+        P.eos[m] = p.materials[m].eos;
+        for (int q = 0; q < TJ_MAX_EOS_PARAMS; ++q) P.prm[m][q] = q < p.materials[m].nparams ? p.materials[m].params[q] : 0.0;
+        P.yield[m] = p.materials[m].yield_stress;
+        if (P.phase[m] == TJ_PHASE_SOLID) P.any_solid = 1;
+    }
+    int M = P.M, n = 0;
+    P.S_ALPHA = n; n += M;
+    P.S_ARHO = n; n += M;
+    P.S_RHOK = n; n += M;
+    P.S_RHO = n++;
+    P.S_RHOU = n; n += 3;
+    P.S_VEL = n; n += 3;
+    P.S_E = n++;
+    P.S_P = n++;
+    P.S_V = P.S_HJ2 = P.S_EPS = P.S_ARE = -1;
+    if (P.solid) { P.S_V = n; n += 9; P.S_HJ2 = n++; }
+    if (P.plastic) { P.S_EPS = n; n += M; P.S_ARE = n; n += M; }
+    P.NS = n;
+    n = 0;
+    P.F_ALPHA = n; n += M;
+    P.F_ARHO = n; n += M;
+    P.F_RHO = n++;
+    P.F_RHOU = n; n += 3;
+    P.F_VEL = n; n += 3;
+    P.F_E = n++;
+    P.F_P = n++;
+    P.F_A = n++;
+    P.F_SIGMA = P.F_V = P.F_ARE = -1;
+    if (P.solid) { P.F_SIGMA = n; n += 9; P.F_V = n; n += 9; }
+    if (P.plastic) { P.F_ARE = n; n += M; }
+    P.NF = n;
+    n = 0;
+    P.X_ALPHA = n; n += M;
+    P.X_ARHO = n; n += M;
+    P.X_RHOU = n; n += 3;
+    P.X_E = n++;
+    P.X_V = P.X_ARE = -1;
+    if (P.solid) { P.X_V = n; n += 9; }
+    if (P.plastic) { P.X_ARE = n; n += M; }
+    P.X_SSTAR = n++;
+    P.X_VSTAR = -1;
+    if (P.solid) { P.X_VSTAR = n; n += 3; }
+    P.NX = n;
+    // AccessPattern (accesspattern.cpp:44-79), no mixtures
+    n = 0;
+    P.A_ALPHA = n; n += M;
+    P.A_ARHO = n; n += M;
+    P.A_RHOK = n; n += M;
+    P.A_RHO = n++;
+    P.A_RHOU = n; n += 3;
+    P.A_VEL = n; n += 3;
+    P.A_E = n++;
+    P.A_P = n++;
+    P.A_A = n++;
+    P.A_USTAR = n++;
+    P.A_SIGMA = n; n += 9;
+    P.A_V = P.A_VSTAR = P.A_DEVH = P.A_HJ2 = P.A_EPS = P.A_ARE = -1;
+    if (P.solid) {
+        P.A_V = n; n += 9;
+        P.A_VSTAR = n; n += 9;
+        P.A_DEVH = n; n += 9;
+        P.A_HJ2 = n++;
+        if (P.plastic) { P.A_EPS = n; n += M; P.A_ARE = n; n += M; }
+    }
+    P.NCOMP = n;
+}
+
+// BoxList::maxSize (AMReX): power-of-two factoring, near-equal chunks chopped
+// from the high end, one direction after another.
+std::vector<int> max_size_boxes(const int* n, int dim, int mgs)
+{
+    std::vector<std::vector<int>> bl{{0, 0, 0, n[0] - 1, n[1] - 1, n[2] - 1}};
+    for (int d = 0; d < dim; ++d) {
+        std::vector<std::vector<int>> out;
+        for (auto b : bl) {
+            int len = b[3 + d] - b[d] + 1;
+            if (len > mgs) {
+                int ratio = 1, bs = mgs, nlen = len;
+                while (bs % 2 == 0 && nlen % 2 == 0) { ratio *= 2; bs /= 2; nlen /= 2; }
+                int numblk = nlen / bs + (nlen % bs ? 1 : 0), sz = nlen / numblk, ex = nlen % numblk;
+                for (int k = 0; k < numblk - 1; ++k) {
+                    int ksize = k < ex ? sz + 1 : sz;
+                    int pos = b[3 + d] - ksize * ratio + 1;
+                    auto up = b;
+                    up[d] = pos;
+                    b[3 + d] = pos - 1;
+                    out.push_back(up);
+                }
+            }
+            out.push_back(b);
+        }
+        bl.swap(out);
+    }
+    std::vector<int> flat;
+    for (auto& b : bl) flat.insert(flat.end(), b.begin(), b.end());
+    return flat;
+}
+
+void free_dev(tj_ctx* c)
+{
+    void* ps[] = {c->d_doms, c->d_boxes, c->d_cell_box, c->A, c->B, c->C, c->UL, c->UR, c->FX, c->ulstar, c->urstar,
+                  c->gstar[0], c->gstar[1], c->gstar[2], c->staging};
+    for (void* p : ps)
+        if (p) cudaFree(p);
+    c->d_doms = nullptr; c->d_boxes = nullptr; c->d_cell_box = nullptr;
+    c->A = c->B = c->C = c->UL = c->UR = c->FX = c->ulstar = c->urstar = nullptr;
+    c->gstar[0] = c->gstar[1] = c->gstar[2] = nullptr;
+    c->staging = nullptr;
+    c->staging_bytes = 0;
+    mixed_free(c->mixed);
+    if (c->graph_exec) { cudaGraphExecDestroy(c->graph_exec); c->graph_exec = nullptr; }
+}
+
+Fp64Bufs bufs(tj_ctx* c)
+{
+    Fp64Bufs b;
+    b.A = c->A; b.B = c->B; b.C = c->C; b.UL = c->UL; b.UR = c->UR; b.FX = c->FX;
+    b.ulstar = c->ulstar; b.urstar = c->urstar;
+    for (int d = 0; d < 3; ++d) { b.gstar[d] = c->gstar[d]; b.nftot[d] = c->nftot[d]; }
+    b.cell_box = c->d_cell_box; b.boxes = c->d_boxes; b.doms = c->d_doms; b.scal = c->d_scal;
+    b.ntot = c->ntot; b.ndom = (int)c->doms.size();
+    return b;
+}
+
+bool is_mixed(const tj_ctx* c) { return c->params.precision == TJ_PRECISION_MIXED; }
+
+// Upload the box table and the cell -> box map (geometry changes only).
+int sync_boxes(tj_ctx* c)
+{
+    std::vector<int> flat;
+    std::vector<int> cell_box(c->ntot);
+    for (size_t q = 0; q < c->doms.size(); ++q) {
+        DevDomain& D = c->doms[q];
+        D.box_off = (int)(flat.size() / 6);
+        D.nbox = (int)(c->boxes[q].size() / 6);
+        flat.insert(flat.end(), c->boxes[q].begin(), c->boxes[q].end());
+        for (int b = 0; b < D.nbox; ++b) {
+            const int* B = &c->boxes[q][6 * b];
+            for (int k = B[2]; k <= B[5]; ++k)
+                for (int j = B[1]; j <= B[4]; ++j)
+                    for (int i = B[0]; i <= B[3]; ++i)
+                        cell_box[D.off + i + (long long)D.n[0] * (j + (long long)D.n[1] * k)] = b;
+        }
+    }
+    if (c->d_boxes) cudaFree(c->d_boxes);
+    TJ_CUDA(c, cudaMalloc(&c->d_boxes, sizeof(int) * std::max<size_t>(flat.size(), 6)));
+    TJ_CUDA(c, cudaMemcpy(c->d_boxes, flat.data(), sizeof(int) * flat.size(), cudaMemcpyHostToDevice));
+    TJ_CUDA(c, cudaMemcpy(c->d_cell_box, cell_box.data(), sizeof(int) * c->ntot, cudaMemcpyHostToDevice));
+    TJ_CUDA(c, cudaMemcpy(c->d_doms, c->doms.data(), sizeof(DevDomain) * c->doms.size(), cudaMemcpyHostToDevice));
+    if (c->graph_exec) { cudaGraphExecDestroy(c->graph_exec); c->graph_exec = nullptr; }
+    if (is_mixed(c)) return mixed_set_boxes(c->mixed, c->P, c->doms, c->boxes, c->stream);
+    return TJ_OK;
+}
+
+int need_state(tj_ctx* c)
+{
+    if (c->doms.empty() || !c->A) return fail(c, TJ_ERR_STATE, "no domain set (tj_set_domains)");
+    return TJ_OK;
+}
+
+int check_status(tj_ctx* c)
+{
+    DevScalars s;
+    TJ_CUDA(c, cudaMemcpyAsync(&s, c->d_scal, sizeof s, cudaMemcpyDeviceToHost, c->stream));
+    TJ_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (s.status != 0) {
+        const char* what = s.status == TJ_ERR_WAVESPEED ? "NaN in wave speeds (hllc.cpp:169-200)"
+                           : s.status == TJ_ERR_ALPHA   ? "error in scaling volume fractions (boxaccesscellarray.cpp:553-588)"
+                           : s.status == TJ_ERR_PLASTIC ? "divide by zero in the plastic update (plastic.cpp:189-193)"
+                           : s.status == TJ_ERR_NAN     ? "NaN found in the state (main.cpp:183-187)"
+                                                        : "device error";
+        return fail(c, s.status, what);
+    }
+    return TJ_OK;
+}
+
+// One full iteration of main.cpp:121-191, device-side dt and t.
+int issue_step(tj_ctx* c)
+{
+    Fp64Bufs b = bufs(c);
+    int n = 0;
+    Prof* pr = c->prof;
+    if (is_mixed(c)) {
+        n += mixed_step(c->mixed, c->P, b, c->stream, pr);
+    } else {
+        n += fp64_cfl(c->P, b, c->A, c->stream, pr);
+        n += fp64_dt_finalize(c->P, b, 1, c->stream);
+        n += fp64_stage(c->P, b, c->A, c->B, 0, c->stream, pr);
+        n += fp64_stage(c->P, b, c->B, c->C, 1, c->stream, pr);
+        n += fp64_step_end(b, c->stream);
+    }
+    c->launches += n;
+    return TJ_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int tj_create(const tj_params* p, tj_ctx** out)
+{
+    if (!p || !out) return TJ_ERR_ARG;
+    *out = nullptr;
+    tj_ctx* c = new tj_ctx();
+    c->params = *p;
+    auto bad = [&](const char* m) {
+        std::fprintf(stderr, "tj_create: %s\n", m);
+        delete c;
+        return TJ_ERR_ARG;
+    };
+    if (p->dim < 1 || p->dim > 3) return bad("dim must be 1, 2 or 3");
+    if (p->n_materials < 1 || p->n_materials > TJ_MAX_MATERIALS) return bad("n_materials out of range");
+    if (p->n_mixtures != 0) return bad("mixtures (MixtureEOS) are not supported");
+    if (p->RADIAL || p->REACTIVE) return bad("RADIAL and REACTIVE are not supported");
+    if (p->nghost < 2) return bad("nghost must be >= 2");
+    if (p->THINC && p->dim == 3) return bad("THINC is 1-D/2-D only in the reference (thinc.cpp:116-127)");
+    if (p->THINC && !p->MUSCL) return bad("THINC needs MUSCL");
+    if (p->THINC && p->SOLID) return bad("THINC with SOLID is not supported");
+    if (p->PLASTIC && !p->SOLID) return bad("PLASTIC needs SOLID");
+    if (p->PLASTIC > 1) return bad("only PLASTIC=1 (radial return) is supported");
+    int any_solid = 0;
+    for (int m = 0; m < p->n_materials; ++m) {
+        const tj_material& mt = p->materials[m];
+        if (mt.eos < 0 || mt.eos > TJ_EOS_HUGONIOT) return bad("unknown EOS");
+        int need = mt.eos == TJ_EOS_MIEGRUNEISEN ? 4 : mt.eos == TJ_EOS_ROMENSKII ? 9 : mt.eos == TJ_EOS_WILKINS ? 11 : 8;
+        if (mt.nparams < need) return bad("too few EOS parameters");
+        if (mt.phase == TJ_PHASE_SOLID) {
+            any_solid = 1;
+            if (mt.eos == TJ_EOS_MIEGRUNEISEN) return bad("a solid needs a solid EOS");
+        }
+    }
+    if (p->SOLID && !any_solid) return bad("SOLID needs a solid material");
+    if (p->precision != TJ_PRECISION_FP64 && p->precision != TJ_PRECISION_MIXED) return bad("unknown precision");
+    if (p->precision == TJ_PRECISION_MIXED && !mixed_supported(*p)) return bad("mixed precision supports fluids only");
+    make_layouts(*p, c->P);
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return bad("no CUDA device");
+    if (cudaMalloc(&c->d_scal, sizeof(DevScalars)) != cudaSuccess) return bad("cudaMalloc failed");
+    DevScalars s;
+    std::memset(&s, 0, sizeof s);
+    s.t_end = 1e300;
+    s.dtmin_bits = 0x7FEFFFFFFFFFFFFFull;
+    cudaMemcpy(c->d_scal, &s, sizeof s, cudaMemcpyHostToDevice);
+    *out = c;
+    return TJ_OK;
+}
+
+int tj_destroy(tj_ctx* c)
+{
+    if (!c) return TJ_OK;
+    cudaStreamSynchronize(c->stream);
+    free_dev(c);
+    delete c->prof;
+    c->prof = nullptr;
+    if (c->d_scal) cudaFree(c->d_scal);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return TJ_OK;
+}
+
+int tj_last_error(const tj_ctx* c, char* buf, unsigned long len)
+{
+    if (!c || !buf || len == 0) return TJ_ERR_ARG;
+    std::snprintf(buf, len, "%s", c->err.c_str());
+    return TJ_OK;
+}
+
+int tj_ncomp(const tj_ctx* c) { return c ? c->P.NCOMP : TJ_ERR_ARG; }
+
+int tj_set_domains(tj_ctx* c, int nd, const int* n_cells, const double* dim_l)
+{
+    if (!c || nd < 1 || !n_cells || !dim_l) return fail(c, TJ_ERR_ARG, "bad domain arguments");
+    TJ_CUDA(c, cudaStreamSynchronize(c->stream));
+    free_dev(c);
+    c->doms.assign(nd, DevDomain());
+    c->boxes.assign(nd, std::vector<int>());
+    long long off = 0, foff[3] = {0, 0, 0};
+    for (int q = 0; q < nd; ++q) {
+        DevDomain& D = c->doms[q];
+        for (int k = 0; k < 3; ++k) {
+            D.n[k] = k < c->P.dim ? n_cells[3 * q + k] : 1;
+            if (D.n[k] < 1) return fail(c, TJ_ERR_ARG, "n_cells must be >= 1");
+            if (k < c->P.dim && D.n[k] < 1) return fail(c, TJ_ERR_ARG, "empty domain");
+            D.dx[k] = (k < c->P.dim ? dim_l[3 * q + k] : (dim_l[3 * q + k] > 0 ? dim_l[3 * q + k] : 1.0)) / (double)D.n[k];
+        }
+        D.off = off;
+        off += (long long)D.n[0] * D.n[1] * D.n[2];
+        for (int d = 0; d < 3; ++d) {
+            D.foff[d] = foff[d];
+            long long nf = (long long)(D.n[0] + (d == 0)) * (D.n[1] + (d == 1)) * (D.n[2] + (d == 2));
+            foff[d] += nf;
+        }
+        c->boxes[q] = {0, 0, 0, D.n[0] - 1, D.n[1] - 1, D.n[2] - 1};
+    }
+    c->ntot = off;
+    for (int d = 0; d < 3; ++d) c->nftot[d] = foff[d];
+    const DevParams& P = c->P;
+    size_t nt = (size_t)c->ntot;
+    TJ_CUDA(c, cudaMalloc(&c->d_doms, sizeof(DevDomain) * nd));
+    TJ_CUDA(c, cudaMalloc(&c->d_cell_box, sizeof(int) * nt));
+    if (is_mixed(c)) {
+        int e = mixed_alloc(c->mixed, P, c->doms, c->ntot, c->nftot, c->stream);
+        if (e) return fail(c, e, "mixed-precision allocation failed");
+        // the FP64 buffers double as the mixed path's conversion staging
+        TJ_CUDA(c, cudaMalloc(&c->A, sizeof(double) * P.NS * nt));
+        TJ_CUDA(c, cudaMemset(c->A, 0, sizeof(double) * P.NS * nt));
+    } else {
+        size_t fmax = (size_t)std::max(c->nftot[0], std::max(c->nftot[1], c->nftot[2]));
+        TJ_CUDA(c, cudaMalloc(&c->A, sizeof(double) * P.NS * nt));
+        TJ_CUDA(c, cudaMalloc(&c->B, sizeof(double) * P.NS * nt));
+        TJ_CUDA(c, cudaMalloc(&c->C, sizeof(double) * P.NS * nt));
+        TJ_CUDA(c, cudaMalloc(&c->UL, sizeof(double) * P.NF * nt));
+        TJ_CUDA(c, cudaMalloc(&c->UR, sizeof(double) * P.NF * nt));
+        TJ_CUDA(c, cudaMalloc(&c->FX, sizeof(double) * P.NX * fmax));
+        TJ_CUDA(c, cudaMemset(c->A, 0, sizeof(double) * P.NS * nt));
+        TJ_CUDA(c, cudaMemset(c->B, 0, sizeof(double) * P.NS * nt));
+        TJ_CUDA(c, cudaMemset(c->C, 0, sizeof(double) * P.NS * nt));
+        if (P.thinc) {
+            TJ_CUDA(c, cudaMalloc(&c->ulstar, sizeof(double) * P.M * nt));
+            TJ_CUDA(c, cudaMalloc(&c->urstar, sizeof(double) * P.M * nt));
+            TJ_CUDA(c, cudaMemset(c->ulstar, 0, sizeof(double) * P.M * nt));
+            TJ_CUDA(c, cudaMemset(c->urstar, 0, sizeof(double) * P.M * nt));
+            for (int d = 0; d < P.dim; ++d) {
+                TJ_CUDA(c, cudaMalloc(&c->gstar[d], sizeof(double) * P.M * c->nftot[d]));
+                TJ_CUDA(c, cudaMemset(c->gstar[d], 0, sizeof(double) * P.M * c->nftot[d]));
+            }
+        }
+    }
+    int e = sync_boxes(c);
+    if (e) return e;
+    return tj_set_time(c, 0.0, 0);
+}
+
+int tj_set_boxes(tj_ctx* c, int q, int nbox, const int* lohi)
+{
+    if (!c || q < 0 || q >= (int)c->doms.size() || nbox < 1 || !lohi) return fail(c, TJ_ERR_ARG, "bad box arguments");
+    const DevDomain& D = c->doms[q];
+    std::vector<int> cover((size_t)D.n[0] * D.n[1] * D.n[2], 0);
+    for (int b = 0; b < nbox; ++b) {
+        const int* B = lohi + 6 * b;
+        for (int k = 0; k < 3; ++k)
+            if (B[k] < 0 || B[3 + k] >= D.n[k] || B[k] > B[3 + k]) return fail(c, TJ_ERR_ARG, "box outside the domain");
+        for (int k = B[2]; k <= B[5]; ++k)
+            for (int j = B[1]; j <= B[4]; ++j)
+                for (int i = B[0]; i <= B[3]; ++i) cover[i + (size_t)D.n[0] * (j + (size_t)D.n[1] * k)]++;
+    }
+    for (int v : cover)
+        if (v != 1) return fail(c, TJ_ERR_ARG, "boxes must tile the domain exactly once");
+    c->boxes[q].assign(lohi, lohi + 6 * nbox);
+    TJ_CUDA(c, cudaStreamSynchronize(c->stream));
+    return sync_boxes(c);
+}
+
+int tj_set_max_grid_size(tj_ctx* c, int q, int mgs)
+{
+    if (!c || q < 0 || q >= (int)c->doms.size() || mgs < 1) return fail(c, TJ_ERR_ARG, "bad max_grid_size");
+    std::vector<int> bl = max_size_boxes(c->doms[q].n, c->P.dim, mgs);
+    return tj_set_boxes(c, q, (int)(bl.size() / 6), bl.data());
+}
+
+int tj_num_boxes(const tj_ctx* c, int q)
+{
+    if (!c || q < 0 || q >= (int)c->doms.size()) return TJ_ERR_ARG;
+    return (int)(c->boxes[q].size() / 6);
+}
+
+int tj_get_box(const tj_ctx* c, int q, int b, int* lohi)
+{
+    if (!c || q < 0 || q >= (int)c->doms.size() || b < 0 || b >= (int)(c->boxes[q].size() / 6) || !lohi) return TJ_ERR_ARG;
+    std::memcpy(lohi, &c->boxes[q][6 * b], 6 * sizeof(int));
+    return TJ_OK;
+}
+
+int tj_num_cells(const tj_ctx* c, long long* n)
+{
+    if (!c || !n) return TJ_ERR_ARG;
+    *n = c->ntot;
+    return TJ_OK;
+}
+
+static int ensure_staging(tj_ctx* c, size_t bytes)
+{
+    if (c->staging_bytes >= bytes) return TJ_OK;
+    if (c->staging) cudaFree(c->staging);
+    c->staging = nullptr;
+    TJ_CUDA(c, cudaMalloc(&c->staging, bytes));
+    c->staging_bytes = bytes;
+    return TJ_OK;
+}
+
+static int exchange(tj_ctx* c, int q, const int* bx, double* host, int ncomp, int ngrow, bool up)
+{
+    int e = need_state(c);
+    if (e) return e;
+    if (ncomp != c->P.NCOMP) return fail(c, TJ_ERR_ARG, "ncomp must equal tj_ncomp()");
+    int dim = c->P.dim;
+    int ld_i = bx[3] - bx[0] + 1 + 2 * ngrow;
+    int ld_j = bx[4] - bx[1] + 1 + (dim > 1 ? 2 * ngrow : 0);
+    int ld_k = bx[5] - bx[2] + 1 + (dim > 2 ? 2 * ngrow : 0);
+    long long cs = (long long)ld_i * ld_j * ld_k;
+    size_t bytes = sizeof(double) * ncomp * cs;
+    e = ensure_staging(c, bytes);
+    if (e) return e;
+    Fp64Bufs b = bufs(c);
+    if (up) {
+        TJ_CUDA(c, cudaMemcpyAsync(c->staging, host, bytes, cudaMemcpyHostToDevice, c->stream));
+        c->launches += fp64_ap_to_state(c->P, b, q, bx, c->staging, ld_i, ld_j, ld_k, cs, ngrow, c->A, c->stream);
+        if (is_mixed(c)) c->launches += mixed_from_fp64(c->mixed, c->P, b, c->stream);
+        TJ_CUDA(c, cudaStreamSynchronize(c->stream));
+    } else {
+        if (is_mixed(c)) c->launches += mixed_to_fp64(c->mixed, c->P, b, c->stream);
+        if (ngrow > 0) TJ_CUDA(c, cudaMemcpyAsync(c->staging, host, bytes, cudaMemcpyHostToDevice, c->stream));
+        c->launches += fp64_state_to_ap(c->P, b, q, bx, c->A, c->staging, ld_i, ld_j, ld_k, cs, ngrow, c->stream);
+        TJ_CUDA(c, cudaMemcpyAsync(host, c->staging, bytes, cudaMemcpyDeviceToHost, c->stream));
+        TJ_CUDA(c, cudaStreamSynchronize(c->stream));
+    }
+    TJ_CUDA(c, cudaGetLastError());
+    return TJ_OK;
+}
+
+int tj_upload_state(tj_ctx* c, int q, int box, const double* fab, int ncomp, int ngrow)
+{
+    if (!c || q < 0 || q >= (int)c->doms.size() || box < 0 || box >= (int)(c->boxes[q].size() / 6) || !fab || ngrow < 0)
+        return fail(c, TJ_ERR_ARG, "bad upload arguments");
+    return exchange(c, q, &c->boxes[q][6 * box], const_cast<double*>(fab), ncomp, ngrow, true);
+}
+
+int tj_download_state(tj_ctx* c, int q, int box, double* fab, int ncomp, int ngrow)
+{
+    if (!c || q < 0 || q >= (int)c->doms.size() || box < 0 || box >= (int)(c->boxes[q].size() / 6) || !fab || ngrow < 0)
+        return fail(c, TJ_ERR_ARG, "bad download arguments");
+    return exchange(c, q, &c->boxes[q][6 * box], fab, ncomp, ngrow, false);
+}
+
+int tj_upload_domain(tj_ctx* c, int q, const double* data)
+{
+    if (!c || q < 0 || q >= (int)c->doms.size() || !data) return fail(c, TJ_ERR_ARG, "bad upload arguments");
+    const DevDomain& D = c->doms[q];
+    int bx[6] = {0, 0, 0, D.n[0] - 1, D.n[1] - 1, D.n[2] - 1};
+    return exchange(c, q, bx, const_cast<double*>(data), c->P.NCOMP, 0, true);
+}
+
+int tj_download_domain(tj_ctx* c, int q, double* data)
+{
+    if (!c || q < 0 || q >= (int)c->doms.size() || !data) return fail(c, TJ_ERR_ARG, "bad download arguments");
+    const DevDomain& D = c->doms[q];
+    int bx[6] = {0, 0, 0, D.n[0] - 1, D.n[1] - 1, D.n[2] - 1};
+    return exchange(c, q, bx, data, c->P.NCOMP, 0, false);
+}
+
+int tj_set_primitive(tj_ctx* c, int q, const double* prim)
+{
+    if (!c || q < 0 || q >= (int)c->doms.size() || !prim) return fail(c, TJ_ERR_ARG, "bad primitive arguments");
+    int e = need_state(c);
+    if (e) return e;
+    const DevDomain& D = c->doms[q];
+    int nprim = 2 * c->P.M + 4 + (c->P.solid ? 9 : 0) + (c->P.plastic ? c->P.M : 0);
+    size_t bytes = sizeof(double) * nprim * (size_t)D.n[0] * D.n[1] * D.n[2];
+    e = ensure_staging(c, bytes);
+    if (e) return e;
+    TJ_CUDA(c, cudaMemcpyAsync(c->staging, prim, bytes, cudaMemcpyHostToDevice, c->stream));
+    Fp64Bufs b = bufs(c);
+    c->launches += fp64_prim_to_state(c->P, b, q, c->staging, c->A, c->stream);
+    if (is_mixed(c)) c->launches += mixed_from_fp64(c->mixed, c->P, b, c->stream);
+    TJ_CUDA(c, cudaStreamSynchronize(c->stream));
+    TJ_CUDA(c, cudaGetLastError());
+    return TJ_OK;
+}
+
+int tj_compute_dt(tj_ctx* c, double* dt)
+{
+    if (!c || !dt) return TJ_ERR_ARG;
+    int e = need_state(c);
+    if (e) return e;
+    Fp64Bufs b = bufs(c);
+    c->launches += fp64_set_dt(b, 0.0, c->stream);
+    if (is_mixed(c)) c->launches += mixed_compute_dt(c->mixed, c->P, b, c->stream);
+    else {
+        c->launches += fp64_cfl(c->P, b, c->A, c->stream);
+        c->launches += fp64_dt_finalize(c->P, b, 0, c->stream);
+    }
+    DevScalars s;
+    TJ_CUDA(c, cudaMemcpyAsync(&s, c->d_scal, sizeof s, cudaMemcpyDeviceToHost, c->stream));
+    TJ_CUDA(c, cudaStreamSynchronize(c->stream));
+    *dt = c->P.cfl * s.dtmin_raw;
+    return TJ_OK;
+}
+
+int tj_advance(tj_ctx* c, double dt)
+{
+    if (!c) return TJ_ERR_ARG;
+    int e = need_state(c);
+    if (e) return e;
+    Fp64Bufs b = bufs(c);
+    c->launches += fp64_set_dt(b, dt, c->stream);
+    if (is_mixed(c)) return fail(c, TJ_ERR_ARG, "tj_advance alone is FP64-only; use tj_step/tj_run in mixed precision");
+    // advance() alone: both stages and the average (finish mode 2), without
+    // the post-advance operators, which have their own entry points.
+    c->launches += fp64_stage(c->P, b, c->A, c->B, 0, c->stream);
+    c->launches += fp64_stage(c->P, b, c->B, c->C, 2, c->stream);
+    TJ_CUDA(c, cudaGetLastError());
+    return check_status(c);
+}
+
+static int cell_op(tj_ctx* c, int op)
+{
+    int e = need_state(c);
+    if (e) return e;
+    Fp64Bufs b = bufs(c);
+    if (is_mixed(c)) c->launches += mixed_to_fp64(c->mixed, c->P, b, c->stream);
+    c->launches += fp64_cell_op(c->P, b, c->A, nullptr, op, c->stream);
+    if (is_mixed(c) && op != OP_NAN) c->launches += mixed_from_fp64(c->mixed, c->P, b, c->stream);
+    TJ_CUDA(c, cudaGetLastError());
+    return check_status(c);
+}
+
+int tj_plastic_update(tj_ctx* c, double dt)
+{
+    (void)dt;
+    if (!c) return TJ_ERR_ARG;
+    if (!c->P.plastic) return TJ_OK;
+    return cell_op(c, OP_PLASTIC);
+}
+int tj_cleanup_v(tj_ctx* c) { return c ? (c->P.solid ? cell_op(c, OP_CLEAN_V) : TJ_OK) : TJ_ERR_ARG; }
+int tj_cleanup_alpha(tj_ctx* c) { return c ? cell_op(c, OP_CLEAN_ALPHA) : TJ_ERR_ARG; }
+int tj_cons_to_prim(tj_ctx* c) { return c ? cell_op(c, OP_C2P) : TJ_ERR_ARG; }
+int tj_prim_to_cons(tj_ctx* c) { return c ? cell_op(c, OP_P2C) : TJ_ERR_ARG; }
+
+int tj_contains_nan(tj_ctx* c, int* flag)
+{
+    if (!c || !flag) return TJ_ERR_ARG;
+    int e = need_state(c);
+    if (e) return e;
+    TJ_CUDA(c, cudaMemsetAsync(&c->d_scal->nan_flag, 0, sizeof(int), c->stream));
+    Fp64Bufs b = bufs(c);
+    if (is_mixed(c)) c->launches += mixed_to_fp64(c->mixed, c->P, b, c->stream);
+    c->launches += fp64_cell_op(c->P, b, c->A, nullptr, OP_NAN, c->stream);
+    DevScalars s;
+    TJ_CUDA(c, cudaMemcpyAsync(&s, c->d_scal, sizeof s, cudaMemcpyDeviceToHost, c->stream));
+    TJ_CUDA(c, cudaStreamSynchronize(c->stream));
+    TJ_CUDA(c, cudaMemsetAsync(&c->d_scal->nan_flag, 0, sizeof(int), c->stream));
+    *flag = s.nan_flag ? 1 : 0;
+    return TJ_OK;
+}
+
+int tj_set_time(tj_ctx* c, double t, int n)
+{
+    if (!c) return TJ_ERR_ARG;
+    DevScalars s;
+    TJ_CUDA(c, cudaMemcpyAsync(&s, c->d_scal, sizeof s, cudaMemcpyDeviceToHost, c->stream));
+    TJ_CUDA(c, cudaStreamSynchronize(c->stream));
+    s.t = t;
+    s.n = n;
+    s.done = 0;
+    s.status = 0;
+    s.nan_flag = 0;
+    s.dtmin_bits = 0x7FEFFFFFFFFFFFFFull;
+    TJ_CUDA(c, cudaMemcpyAsync(c->d_scal, &s, sizeof s, cudaMemcpyHostToDevice, c->stream));
+    TJ_CUDA(c, cudaStreamSynchronize(c->stream));
+    return TJ_OK;
+}
+
+int tj_get_time(tj_ctx* c, double* t, int* n, double* last_dt)
+{
+    if (!c) return TJ_ERR_ARG;
+    DevScalars s;
+    TJ_CUDA(c, cudaMemcpyAsync(&s, c->d_scal, sizeof s, cudaMemcpyDeviceToHost, c->stream));
+    TJ_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (t) *t = s.t;
+    if (n) *n = s.n;
+    if (last_dt) *last_dt = s.dt;
+    return TJ_OK;
+}
+
+static int set_t_end(tj_ctx* c, double t_end)
+{
+    // t_end lives in the scalars block; a tiny host->device write of one field
+    TJ_CUDA(c, cudaMemcpyAsync(&c->d_scal->t_end, &t_end, sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    TJ_CUDA(c, cudaStreamSynchronize(c->stream));
+    return TJ_OK;
+}
+
+int tj_step(tj_ctx* c, double t_end)
+{
+    if (!c) return TJ_ERR_ARG;
+    int e = need_state(c);
+    if (e) return e;
+    e = set_t_end(c, t_end);
+    if (e) return e;
+    issue_step(c);
+    TJ_CUDA(c, cudaGetLastError());
+    return TJ_OK;
+}
+
+int tj_run(tj_ctx* c, int nsteps, double t_end, int* steps_done, double* t_out)
+{
+    if (!c || nsteps < 0) return TJ_ERR_ARG;
+    int e = need_state(c);
+    if (e) return e;
+    e = set_t_end(c, t_end);
+    if (e) return e;
+    int n0 = 0;
+    double t0 = 0;
+    e = tj_get_time(c, &t0, &n0, nullptr);
+    if (e) return e;
+    const int group = 20;
+    long long per_group = 0;
+    if (!c->graph_exec || c->graph_steps != group) {
+        if (c->graph_exec) { cudaGraphExecDestroy(c->graph_exec); c->graph_exec = nullptr; }
+        cudaGraph_t g;
+        long long before = c->launches;
+        if (c->prof) {
+            c->prof->collect_direct();
+            c->prof->reserve((size_t)group * 64 + 256);
+            c->prof->cursor = 0;
+            c->prof->capturing = true;
+        }
+        TJ_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        for (int s = 0; s < group; ++s) issue_step(c);
+        TJ_CUDA(c, cudaStreamEndCapture(c->stream, &g));
+        TJ_CUDA(c, cudaGraphInstantiate(&c->graph_exec, g, 0));
+        cudaGraphDestroy(g);
+        if (c->prof) {
+            c->prof->capturing = false;
+            c->prof->graph_end = c->prof->cursor;
+        }
+        per_group = c->launches - before;
+        c->launches = before;  // counted when launched
+        c->graph_steps = group;
+        c->graph_launches = per_group;
+    }
+    per_group = c->graph_launches;
+    int remaining = nsteps;
+    int n = n0;
+    double t = t0;
+    while (remaining > 0) {
+        bool graph = remaining >= group;
+        if (graph) {
+            TJ_CUDA(c, cudaGraphLaunch(c->graph_exec, c->stream));
+            c->launches += per_group;
+            remaining -= group;
+        } else {
+            for (int s = 0; s < remaining; ++s) issue_step(c);
+            remaining = 0;
+        }
+        e = tj_get_time(c, &t, &n, nullptr);
+        if (e) return e;
+        if (c->prof) {
+            if (graph) c->prof->collect(0, c->prof->graph_end);
+            else c->prof->collect_direct();
+        }
+        DevScalars s;
+        TJ_CUDA(c, cudaMemcpyAsync(&s, c->d_scal, sizeof s, cudaMemcpyDeviceToHost, c->stream));
+        TJ_CUDA(c, cudaStreamSynchronize(c->stream));
+        if (s.done) break;
+    }
+    if (steps_done) *steps_done = n - n0;
+    if (t_out) *t_out = t;
+    TJ_CUDA(c, cudaGetLastError());
+    return check_status(c);
+}
+
+int tj_status(tj_ctx* c)
+{
+    if (!c) return TJ_ERR_ARG;
+    return check_status(c);
+}
+
+int tj_synchronize(tj_ctx* c)
+{
+    if (!c) return TJ_ERR_ARG;
+    TJ_CUDA(c, cudaStreamSynchronize(c->stream));
+    return TJ_OK;
+}
+
+int tj_launch_count(const tj_ctx* c, long long* count)
+{
+    if (!c || !count) return TJ_ERR_ARG;
+    *count = c->launches;
+    return TJ_OK;
+}
+
+int tj_get_stream(tj_ctx* c, void** stream)
+{
+    if (!c || !stream) return TJ_ERR_ARG;
+    *stream = (void*)c->stream;
+    return TJ_OK;
+}
+
+int tj_set_profiling(tj_ctx* c, int on)
+{
+    if (!c) return TJ_ERR_ARG;
+    TJ_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (c->graph_exec) { cudaGraphExecDestroy(c->graph_exec); c->graph_exec = nullptr; }
+    if (on && !c->prof) c->prof = new EventProf();
+    if (!on && c->prof) { delete c->prof; c->prof = nullptr; }
+    return TJ_OK;
+}
+
+int tj_kernel_time(tj_ctx* c, const char* kernel, double* ms_total, long long* launches)
+{
+    if (!c || !kernel) return TJ_ERR_ARG;
+    if (ms_total) *ms_total = 0.0;
+    if (launches) *launches = 0;
+    if (!c->prof) return TJ_OK;
+    TJ_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->prof->collect_direct();
+    for (auto& t : c->prof->totals)
+        if (t.first == kernel && ms_total) *ms_total = t.second;
+    for (auto& n : c->prof->counts)
+        if (n.first == kernel && launches) *launches = n.second;
+    return TJ_OK;
+}
+
+}  // extern "C"

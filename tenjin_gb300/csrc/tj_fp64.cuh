@@ -1,0 +1,42 @@
+// FP64 reference-faithful kernels of the per-timestep update.
+#pragma once
+
+#include "tj_types.h"
+
+namespace tj {
+
+struct Fp64Bufs {
+    double *A, *B, *C;        // state: U^n (and result), stage-1 output, stage-2 partial
+    double *UL, *UR;          // reconstructed face states, one per cell
+    double* FX;               // face fluxes of the current direction
+    double *ulstar, *urstar;  // THINC scratch (alpha of the reference's ULStar / URStar)
+    double* gstar[3];         // ULStar ghost alpha at box hi+1 faces, per direction
+    int* cell_box;            // domain-local box index of each cell
+    int* boxes;               // 6 ints per box, all domains
+    DevDomain* doms;
+    DevScalars* scal;
+    long long ntot, nftot[3];
+    int ndom;
+};
+
+// Launch helpers (tj_fp64.cu). Each returns the number of kernel launches.
+int fp64_cfl(const DevParams& P, const Fp64Bufs& b, const double* X, cudaStream_t st, Prof* pr = nullptr);
+int fp64_dt_finalize(const DevParams& P, const Fp64Bufs& b, int use_clamp, cudaStream_t st);
+int fp64_stage(const DevParams& P, const Fp64Bufs& b, const double* X, double* Y, int finish, cudaStream_t st,
+               Prof* pr = nullptr);
+int fp64_step_end(const Fp64Bufs& b, cudaStream_t st);
+int fp64_set_dt(const Fp64Bufs& b, double dt, cudaStream_t st);
+
+// Whole-array operators of the C ABI.
+enum CellOp { OP_C2P = 0, OP_P2C = 1, OP_CLEAN_ALPHA = 2, OP_CLEAN_V = 3, OP_PLASTIC = 4, OP_NAN = 5, OP_AVERAGE = 6 };
+int fp64_cell_op(const DevParams& P, const Fp64Bufs& b, double* X, const double* X2, int op, cudaStream_t st);
+
+// Layout conversion: AccessPattern blocks (valid cells of one box of one
+// domain, ncomp x box cells, i fastest) <-> carried state.
+int fp64_ap_to_state(const DevParams& P, const Fp64Bufs& b, int dom, const int* box_lohi, const double* ap, int ld_i,
+                     int ld_j, int ld_k, long long cstride, int ghost_off, double* X, cudaStream_t st);
+int fp64_state_to_ap(const DevParams& P, const Fp64Bufs& b, int dom, const int* box_lohi, const double* X, double* ap,
+                     int ld_i, int ld_j, int ld_k, long long cstride, int ghost_off, cudaStream_t st);
+int fp64_prim_to_state(const DevParams& P, const Fp64Bufs& b, int dom, const double* prim, double* X, cudaStream_t st);
+
+}  // namespace tj

@@ -1,0 +1,54 @@
+// Internal types shared by the host C-ABI layer and the kernels.
+#pragma once
+
+#include "tenjin_gpu.h"
+
+#define TJ_MAX_MAT TJ_MAX_MATERIALS
+
+namespace tj {
+
+// Device copy of the solver parameters plus the layouts of the device
+// arrays (component offsets). Passed to kernels by value.
+struct DevParams {
+    int dim, M, solid, thinc, plastic, muscl, any_solid;
+    int lo_bc[3], hi_bc[3];
+    double cfl, beta;
+    int phase[TJ_MAX_MAT], eos[TJ_MAX_MAT];
+    double prm[TJ_MAX_MAT][TJ_MAX_EOS_PARAMS];
+    double yield[TJ_MAX_MAT];
+    // carried state (one SoA block of ntot cells per word)
+    int S_ALPHA, S_ARHO, S_RHOK, S_RHO, S_RHOU, S_VEL, S_E, S_P, S_V, S_HJ2, S_EPS, S_ARE, NS;
+    // reconstructed face state (UL / UR)
+    int F_ALPHA, F_ARHO, F_RHO, F_RHOU, F_VEL, F_E, F_P, F_A, F_SIGMA, F_V, F_ARE, NF;
+    // face flux
+    int X_ALPHA, X_ARHO, X_RHOU, X_E, X_SSTAR, X_V, X_VSTAR, X_ARE, NX;
+    // AccessPattern (reference component order)
+    int A_ALPHA, A_ARHO, A_RHOK, A_RHO, A_RHOU, A_VEL, A_E, A_P, A_A, A_USTAR, A_SIGMA, A_V, A_VSTAR, A_DEVH, A_HJ2,
+        A_EPS, A_ARE, NCOMP;
+};
+
+// One independent domain: valid cells [0,n) per axis, stored contiguously
+// from cell offset `off` (i fastest) in every state block.
+struct DevDomain {
+    int n[3];
+    double dx[3];
+    long long off;        // first cell in the concatenated cell space
+    long long foff[3];    // first face of direction d in the face space of d
+    int box_off, nbox;    // range in the box table
+};
+
+// Scalars kept on the device for graph-captured time stepping.
+struct DevScalars {
+    double t, dt, t_end, dtmin_raw;
+    unsigned long long dtmin_bits;  // atomicMin over positive doubles as bits
+    int n, status, done, nan_flag;
+};
+
+// Launch-timing hook: begin/end bracket one kernel launch on a stream.
+struct Prof {
+    virtual void begin(const char* kernel, void* stream) = 0;
+    virtual void end(const char* kernel, void* stream) = 0;
+    virtual ~Prof() {}
+};
+
+}  // namespace tj

@@ -1,0 +1,82 @@
+"""Generate the golden fixtures of tests/golden/ by running the REFERENCE'S
+OWN hot-path sources (compiled from the reference tree through oracle/Makefile
+into oracle/_ref/) on seeded synthetic inputs.
+
+Run where the reference tree exists:  python tests/golden/make_golden.py
+Each fixture stores the builder call that makes its input, a SHA-256 of the
+initial primitive fields, the dt of every step and the final values of the
+carried components (AccessPattern indices listed in the file).
+"""
+import hashlib
+import json
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from tenjin_gb300 import cases  # noqa: E402
+from tenjin_gb300.host import carried_components  # noqa: E402
+from oracle import refio  # noqa: E402
+
+FIXTURES = {
+    "sod1000_full": ("sod_1d", {}),
+    "sod200_boxes": ("sod_1d", {"ncells": 200, "max_grid_size": 37, "max_steps": 60}),
+    "sod_thinc_1d": ("sod_1d", {"ncells": 100, "max_grid_size": 30, "max_steps": 80}, {"thinc": 1}),
+    "bubble48_thinc_uneven": ("shock_bubble_2d", {"n": 48, "max_grid_size": 20, "max_steps": 60, "radius": 0.3}),
+    "bubble64_thinc": ("shock_bubble_2d", {"n": 64, "max_grid_size": 32, "max_steps": 40}),
+    "bubble40_reflect": ("shock_bubble_2d", {"n": 40, "max_grid_size": 16, "max_steps": 40, "radius": 0.3},
+                         {"lo_bc": [1, 1, 0], "hi_bc": [1, 0, 0]}),
+    "bubble32_muscl": ("shock_bubble_2d", {"n": 32, "max_grid_size": 32, "max_steps": 30, "thinc": 0}),
+    "uneven3d_4dom": ("uneven_boxes_3d", {"nbox": 4, "lo": 6, "hi": 10, "max_steps": 8}),
+    "fluid3d_boxes": ("fluid_boxes_3d", {"n": 12, "max_grid_size": 5, "max_steps": 5}),
+    "copper12": ("copper_plate_3d", {"n": 12, "max_grid_size": 6, "max_steps": 8}),
+    "wilkins2d_plastic": ("solid_mixture_2d", {"eos": cases.EOS_WILKINS, "n": 20, "max_steps": 10}),
+    "romenskii2d_plastic": ("solid_mixture_2d", {"eos": cases.EOS_ROMENSKII, "n": 20, "max_steps": 10}),
+    "hugoniot2d_plastic": ("solid_mixture_2d", {"eos": cases.EOS_HUGONIOT, "n": 16, "max_steps": 10}),
+}
+
+
+def build_case(name):
+    spec = FIXTURES[name]
+    c = getattr(cases, spec[0])(**spec[1])
+    for k, v in (spec[2] if len(spec) > 2 else {}).items():
+        setattr(c, k, v)
+    return c
+
+
+def prim_sha(c):
+    h = hashlib.sha256()
+    for d in c.domains:
+        h.update(np.ascontiguousarray(d.prim, dtype="<f8").tobytes())
+    return h.hexdigest()
+
+
+def main():
+    subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "-j3"], check=True)
+    manifest = {}
+    for name in FIXTURES:
+        c = build_case(name)
+        out = refio.run_reference(c)
+        if out["nan_stop"]:
+            raise RuntimeError(f"{name}: reference stopped on NaN")
+        idx = carried_components(c)
+        arrs = {"dts": out["dts"], "carried": np.array(idx, dtype=np.int32)}
+        for q, st in enumerate(out["states"]):
+            arrs[f"state_{q}"] = st[idx]
+        np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **arrs)
+        spec = FIXTURES[name]
+        manifest[name] = {"builder": spec[0], "kwargs": spec[1], "overrides": spec[2] if len(spec) > 2 else {},
+                          "prim_sha256": prim_sha(c), "steps": int(len(out["dts"])), "t": out["t"]}
+        print(f"{name}: {len(out['dts'])} steps, t={out['t']:.6g}")
+    with open(os.path.join(HERE, "manifest.json"), "w") as f:
+        json.dump({"generator": "reference sources through oracle/Makefile (serial, -O2 -ffp-contract=off)",
+                   "fixtures": manifest}, f, indent=1, sort_keys=True)
+
+
+if __name__ == "__main__":
+    main()

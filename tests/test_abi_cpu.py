@@ -1,0 +1,63 @@
+"""The C-ABI library builds, loads and exports every entry point that
+include/tenjin_gpu.h declares; host-side argument checks (no GPU needed)."""
+import ctypes
+import os
+import re
+import subprocess
+
+import pytest
+
+from tenjin_gb300 import _lib, build, cases
+from tenjin_gb300.host import make_params
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    build.build()
+    return _lib.load()
+
+
+def declared_symbols():
+    with open(os.path.join(ROOT, "include", "tenjin_gpu.h")) as f:
+        src = f.read()
+    return sorted(set(re.findall(r"^int\s+(tj_\w+)\s*\(", src, flags=re.M)))
+
+
+def test_every_declared_symbol_is_exported(lib):
+    out = subprocess.run(["nm", "-D", "--defined-only", build.LIB], capture_output=True, text=True, check=True).stdout
+    exported = set(re.findall(r"\bT (tj_\w+)", out))
+    missing = [s for s in declared_symbols() if s not in exported]
+    assert not missing, missing
+    assert {name for name, _, _ in _lib.SIGNATURES} == set(declared_symbols())
+
+
+def test_library_targets_sm_103a():
+    out = subprocess.run(["cuobjdump", "--list-elf", build.LIB], capture_output=True, text=True)
+    if out.returncode != 0:
+        pytest.skip("cuobjdump unavailable")
+    assert "sm_103a" in out.stdout
+
+
+@pytest.mark.parametrize("mutate,why", [
+    (lambda p: setattr(p, "dim", 4), "dim"),
+    (lambda p: setattr(p, "n_mixtures", 1), "mixtures"),
+    (lambda p: setattr(p, "RADIAL", 1), "radial"),
+    (lambda p: setattr(p, "nghost", 1), "nghost"),
+    (lambda p: setattr(p, "n_materials", 5), "materials"),
+])
+def test_create_rejects_unsupported_parameters(lib, mutate, why):
+    p = make_params(cases.sod_1d(ncells=10))
+    mutate(p)
+    h = ctypes.c_void_p()
+    assert lib.tj_create(ctypes.byref(p), ctypes.byref(h)) == -1
+    assert not h.value
+
+
+def test_create_rejects_thinc_in_3d(lib):
+    c = cases.uneven_boxes_3d(nbox=1, lo=4, hi=4)
+    c.thinc = 1
+    p = make_params(c)
+    h = ctypes.c_void_p()
+    assert lib.tj_create(ctypes.byref(p), ctypes.byref(h)) == -1

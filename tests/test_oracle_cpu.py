@@ -1,0 +1,82 @@
+"""The oracle (the CPU port of oracle/port/) against the golden fixtures made
+by the reference's own sources, and against independent checks."""
+import os
+
+import numpy as np
+import pytest
+
+import fixtures as fx
+import exact_riemann as er
+from oracle import port, refio
+from tenjin_gb300 import cases
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    port.build_port()
+
+
+@pytest.mark.parametrize("name", fx.names())
+def test_fixture_inputs_are_reproducible(name):
+    c = fx.build_case(name)
+    assert fx.prim_sha(c) == fx.manifest()[name]["prim_sha256"]
+
+
+@pytest.mark.parametrize("name", fx.names())
+def test_port_bit_exact_against_reference_fixture(name):
+    c = fx.build_case(name)
+    gold = fx.load(name)
+    out = port.run_port(c)
+    np.testing.assert_array_equal(out["dts"], gold["dts"])
+    for q, st in enumerate(out["states"]):
+        got = st[gold["carried"]]
+        assert fx.exact_fraction(got, gold["states"][q]) == 1.0, f"domain {q}: max rel diff {fx.rel_diff(got, gold['states'][q])}"
+
+
+def test_sod_matches_exact_riemann_solution():
+    gold = fx.load("sod1000_full")
+    c = fx.build_case("sod1000_full")
+    M = c.M
+    rho = gold["states"][0][gold["carried"].index(3 * M)][0, 0]
+    x = (np.arange(1000) + 0.5) / 1000
+    re, ue, pe = er.sample(x, 0.2, 0.5, 1.0, 0.0, 1.0, 0.125, 0.0, 0.1)
+    assert abs(float(np.sum(gold["dts"])) - 0.2) < 1e-14
+    assert np.mean(np.abs(rho - re)) < 2e-3
+
+
+def test_planted_mistake_is_caught():
+    """A wrong CFL number in the oracle must break the bit-exact comparison."""
+    c = fx.build_case("sod200_boxes")
+    c.cfl = 0.5 * (1 + 1e-12)
+    gold = fx.load("sod200_boxes")
+    out = port.run_port(c)
+    assert not np.array_equal(out["dts"], gold["dts"])
+
+
+def test_mass_conservation_quiet_boundaries():
+    """An over-pressured bubble in water at rest: until the waves reach the
+    walls no mass crosses the boundary, so each total alphaRho is conserved to
+    round-off (the interior update is conservative, hllc.cpp:493-523)."""
+    c = cases.shock_bubble_2d(n=32, max_grid_size=16, max_steps=10, radius=0.2, shock_x=-1.0)
+    d = c.domains[0]
+    d.prim[7] = np.where(d.prim[1] > 0.5, 3.0e5, d.prim[7])
+    sim = port.PortSim(c)
+    st0 = sim.state(0)
+    out = sim.run()
+    st1 = out["states"][0]
+    M = c.M
+    for m in range(M):
+        m0, m1 = st0[M + m].sum(), st1[M + m].sum()
+        assert abs(m1 - m0) / abs(m0) < 1e-11
+
+
+@pytest.mark.skipif(not refio.have_ref(2), reason="reference binaries are built only where the reference tree exists")
+def test_port_matches_live_reference_random_inputs():
+    rng = np.random.default_rng(7)
+    c = cases.shock_bubble_2d(n=24, max_grid_size=9, max_steps=12, radius=0.25)
+    d = c.domains[0]
+    d.prim[7] *= 1.0 + 0.05 * rng.standard_normal(d.prim[7].shape)
+    r = refio.run_reference(c)
+    p = port.run_port(c)
+    np.testing.assert_array_equal(r["dts"], p["dts"])
+    assert fx.exact_fraction(p["states"][0], r["states"][0]) == 1.0
