@@ -48,14 +48,21 @@ struct EventProf : Prof {
             reserve(pool.size() + 256);
         }
         pool[cursor].name = kernel;
-        cudaEventRecord(pool[cursor].a, (cudaStream_t)st);
+        record(pool[cursor].a, st);
     }
     void end(const char* kernel, void* st) override
     {
         (void)kernel;
         if (cursor >= pool.size()) return;
-        cudaEventRecord(pool[cursor].b, (cudaStream_t)st);
+        record(pool[cursor].b, st);
         ++cursor;
+    }
+    // Inside a stream capture an event must be recorded as an external event
+    // node to be recorded again each time the graph runs.
+    void record(cudaEvent_t e, void* st)
+    {
+        if (capturing) cudaEventRecordWithFlags(e, (cudaStream_t)st, cudaEventRecordExternal);
+        else cudaEventRecord(e, (cudaStream_t)st);
     }
     void add(const std::string& n, double ms)
     {
@@ -70,6 +77,7 @@ struct EventProf : Prof {
         for (size_t i = lo; i < hi && i < pool.size(); ++i) {
             float ms = 0.f;
             if (cudaEventElapsedTime(&ms, pool[i].a, pool[i].b) == cudaSuccess) add(pool[i].name, ms);
+            else cudaGetLastError();  // a pair that was not recorded: skip it
         }
     }
     void collect_direct()
@@ -616,8 +624,11 @@ int tj_compute_dt(tj_ctx* c, double* dt)
     if (e) return e;
     Fp64Bufs b = bufs(c);
     c->launches += fp64_set_dt(b, 0.0, c->stream);
-    if (is_mixed(c)) c->launches += mixed_compute_dt(c->mixed, c->P, b, c->stream);
-    else {
+    if (is_mixed(c)) {
+        c->launches += mixed_compute_dt(c->mixed, c->P, b, c->stream);
+        c->launches += fp64_dt_finalize(c->P, b, 0, c->stream);
+        c->launches += mixed_compute_dt(c->mixed, c->P, b, c->stream);  // re-arm for the next step
+    } else {
         c->launches += fp64_cfl(c->P, b, c->A, c->stream);
         c->launches += fp64_dt_finalize(c->P, b, 0, c->stream);
     }

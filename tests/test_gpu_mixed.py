@@ -1,0 +1,63 @@
+"""Mixed-precision path (binary32 bulk, compensated energy, binary64 pressure
+closure) against the FP64 reference-faithful path on the same inputs. The
+stated bound is the relative L1 error of the density field (sum of
+alphaRho): <= 1e-4."""
+import numpy as np
+import pytest
+
+from tenjin_gb300 import build, cases
+from tenjin_gb300.host import FP64, MIXED, TenjinGPU
+
+pytestmark = pytest.mark.gpu
+L1_TOL = 1e-4
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built():
+    build.build()
+
+
+def density(st, M):
+    return st[M:2 * M].sum(axis=0)
+
+
+def run(c, precision, steps):
+    g = TenjinGPU(c, precision)
+    done, t = g.run(steps, 1e300)
+    st = g.state(0)
+    return done, t, st
+
+
+@pytest.mark.parametrize("thinc,n,mgs,steps", [(1, 128, 64, 60), (0, 128, 128, 60), (1, 96, 40, 40)])
+def test_mixed_density_l1_against_fp64(thinc, n, mgs, steps):
+    c = cases.shock_bubble_2d(n=n, max_grid_size=mgs, max_steps=steps, thinc=thinc)
+    d64, t64, s64 = run(c, FP64, steps)
+    d32, t32, s32 = run(c, MIXED, steps)
+    assert d64 == d32 == steps
+    assert abs(t32 - t64) <= 1e-5 * t64
+    r64, r32 = density(s64, c.M), density(s32, c.M)
+    assert np.all(np.isfinite(r32))
+    l1 = np.abs(r32 - r64).sum() / np.abs(r64).sum()
+    assert l1 <= L1_TOL, f"relative L1 density error {l1:.3e}"
+
+
+def test_mixed_conserves_mass_with_quiet_boundaries():
+    c = cases.shock_bubble_2d(n=64, max_grid_size=32, max_steps=20, shock_x=-1.0)
+    d = c.domains[0]
+    d.prim[7] = np.where(d.prim[1] > 0.5, 3.0e5, d.prim[7])
+    g = TenjinGPU(c, MIXED)
+    s0 = g.state(0)
+    g.run(20, 1e300)
+    s1 = g.state(0)
+    for m in range(c.M):
+        m0, m1 = s0[c.M + m].sum(), s1[c.M + m].sum()
+        assert abs(m1 - m0) / abs(m0) < 1e-6
+
+
+def test_mixed_reflective_walls_run():
+    c = cases.shock_bubble_2d(n=64, max_grid_size=32, max_steps=30)
+    c.lo_bc, c.hi_bc = [1, 1, 0], [1, 1, 0]
+    d64, _, s64 = run(c, FP64, 30)
+    d32, _, s32 = run(c, MIXED, 30)
+    r64, r32 = density(s64, c.M), density(s32, c.M)
+    assert np.abs(r32 - r64).sum() / np.abs(r64).sum() <= L1_TOL
