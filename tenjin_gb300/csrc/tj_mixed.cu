@@ -225,18 +225,21 @@ struct Cand {
     float L[TJ_MAX_MAT], R[TJ_MAX_MAT];
 };
 
+// Boundary image of index i (foextrap: nearest cell; reflect: mirror). Images
+// deeper than the domain is wide are clamped into it; only ghost depths up to
+// two are ever consumed.
 __device__ __forceinline__ int reflect_map(int i, int n, int lo_bc, int hi_bc, bool& refl)
 {
     refl = false;
+    int j = i;
     if (i < 0) {
-        if (lo_bc == TJ_BC_REFLECTIVE) { refl = true; return -1 - i; }
-        return 0;
+        if (lo_bc == TJ_BC_REFLECTIVE) { refl = true; j = -1 - i; }
+        else j = 0;
+    } else if (i > n - 1) {
+        if (hi_bc == TJ_BC_REFLECTIVE) { refl = true; j = 2 * n - 1 - i; }
+        else j = n - 1;
     }
-    if (i > n - 1) {
-        if (hi_bc == TJ_BC_REFLECTIVE) { refl = true; return 2 * n - 1 - i; }
-        return n - 1;
-    }
-    return i;
+    return j < 0 ? 0 : (j > n - 1 ? n - 1 : j);
 }
 
 __device__ __forceinline__ float ur_read(const MixB& b, int m, long long c, int s)
