@@ -164,6 +164,22 @@ int tj_get_stream(tj_ctx* ctx, void** stream);
 int tj_set_profiling(tj_ctx* ctx, int on);
 int tj_kernel_time(tj_ctx* ctx, const char* kernel, double* ms_total, long long* launches);
 
+/* Time step without any device allocation. No counterpart in the reference:
+ * it exists for callers that cannot allocate device memory themselves (a
+ * host whose framework owns the GPU's memory pool, a plugin restricted to the
+ * buffers its host hands it, a running loop that must not allocate). Needs no
+ * context. state: DEVICE pointer to one domain's state in the AccessPattern
+ * layout (tj_ncomp blocks of nx*ny*nz doubles, i fastest); dt: HOST pointer
+ * receiving CFL * min(dx/(a+|u|)) as tj_compute_dt computes it; stream: the
+ * cudaStream_t to order the work on (NULL: the default stream). Working
+ * memory is a fixed array inside the library (TJ_NOALLOC_MAX_CELLS bounds the
+ * domain; larger domains return TJ_ERR_ARG). The first call on a device looks
+ * up that array's address; make it before any stream capture. Calls that
+ * overlap on the GPU share the array and race: serialise them. */
+#define TJ_NOALLOC_MAX_CELLS (1 << 24)
+int tj_compute_dt_noalloc(const tj_params* params, const int* n_cells, const double* dim_l, const double* state,
+                          double* dt, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -77,6 +77,7 @@ SIGNATURES = [
     ("tj_get_stream", _I, [_P, ctypes.POINTER(_P)]),
     ("tj_set_profiling", _I, [_P, _I]),
     ("tj_kernel_time", _I, [_P, ctypes.c_char_p, _PD, ctypes.POINTER(ctypes.c_longlong)]),
+    ("tj_compute_dt_noalloc", _I, [ctypes.POINTER(TjParams), _PI, _PD, ctypes.c_void_p, _PD, ctypes.c_void_p]),
 ]
 
 _lib = None

@@ -25,6 +25,7 @@ UNITS = {
     "tj_api.cu": [],
     "tj_fp64.cu": ["-fmad=false"],
     "tj_mixed.cu": [],
+    "tj_noalloc.cu": ["-fmad=false"],
 }
 
 
