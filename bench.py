@@ -234,6 +234,34 @@ def run_gpu_arm(args):
                "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes, "steps": args.e2e_steps,
                "path": "tj_upload_domain + tj_step + tj_download_domain (AccessPattern layout, pinned host)"}
 
+    # FP32 vs FP64: the FP64 path on the same workload and step count (not
+    # part of the timed region): its throughput and the relative L1 error of
+    # the density field (sum of alphaRho) of the mixed result against it
+    fp64 = None
+    if precision == MIXED and args.fp64_compare:
+        M = case.M
+        dens32 = g.state(0)[M:2 * M].sum(axis=0)
+        g64 = TenjinGPU(case, FP64)
+        sp64 = ctypes.c_void_p()
+        lib.tj_get_stream(g64.h, ctypes.byref(sp64))
+        st64 = torch.cuda.ExternalStream(sp64.value)
+        g64.run(args.warmup + 1, 1e300)
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(st64):
+            f0.record(st64)
+        g64.run(args.steps, 1e300)
+        with torch.cuda.stream(st64):
+            f1.record(st64)
+        torch.cuda.synchronize()
+        ms64 = f0.elapsed_time(f1)
+        dens64 = g64.state(0)[M:2 * M].sum(axis=0)
+        t32 = g.time()[0]
+        t64 = g64.time()[0]
+        g64.close()
+        fp64 = {"value": ncell * args.steps / (ms64 / 1e3), "unit": "cell-updates/s", "ms_per_step": ms64 / args.steps,
+                "l1_rel_density_err": float(abs(dens32 - dens64).sum() / abs(dens64).sum()),
+                "linf_rel_density_err": float(abs(dens32 - dens64).max() / abs(dens64).max()),
+                "steps_compared": args.warmup + 1 + args.steps, "t_mixed": t32, "t_fp64": t64}
     g.close()
     value = ncell * args.steps * ws / (ms / 1e3)
     line = {
@@ -245,6 +273,7 @@ def run_gpu_arm(args):
                    "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
                    "l2": "state working set larger than L2 (three state buffers of >= 48 MB plus scratch per step)"},
         "gpu_launches": launches, "steps_done": done, "e2e": e2e, "roofline": roofline, "clocks": clocks,
+        "fp64": fp64,
     }
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
@@ -325,7 +354,8 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["mixed", "fp64"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--no-fp64-compare", dest="fp64_compare", action="store_false")
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -52,7 +52,8 @@ struct MixP {
     int lo_bc[2], hi_bc[2];
     float dx[2], beta;
     float g[TJ_MAX_MAT], ig[TJ_MAX_MAT], pref[TJ_MAX_MAT], eref[TJ_MAX_MAT];
-    double cE[TJ_MAX_MAT], eE[TJ_MAX_MAT];
+    // pref/Gamma and eref as float pairs (hi + lo) for the pressure closure
+    float cEh[TJ_MAX_MAT], cEl[TJ_MAX_MAT], eEh[TJ_MAX_MAT], eEl[TJ_MAX_MAT];
     double cfl;
     int last_box[4];  // lo x, lo y, hi x, hi y of the last box in MFIter order
 };
@@ -88,18 +89,36 @@ struct FaceS {
     float a[M], ar[M], rho, ru[2], u[2], E, p, c;
 };
 
+// MUSCL slope (hllc.cpp:527-568). With a = u0-um, b = up-u0 and r = a/b, the
+// reference's limiter phi(r) = min(2/(1+r), 2r/(1+r)) for r > 0 (0 for r <= 0,
+// inf or NaN) applied to (up-um)/2 equals, in exact arithmetic, the argument
+// of smaller magnitude when a and b have the same sign and 0 otherwise; the
+// binary32 path evaluates that division-free form.
 __device__ __forceinline__ void muscl_f(float um, float u0, float up, float& l, float& r)
 {
-    float rr = (u0 - um) / (up - u0);
-    if (!isfinite(rr)) rr = 0.f;
-    float phi = 0.f;
-    if (rr > 0.f) {
-        float a = 2.f / (1.f + rr), b = 2.f * rr / (1.f + rr);
-        phi = (b < a) ? b : a;
-    }
-    float g = phi * 0.5f * (up - um);
+    const float a = u0 - um, b = up - u0;
+    float g = 0.f;
+    if (a * b > 0.f) g = (fabsf(a) < fabsf(b)) ? a : b;
     l = u0 - 0.5f * g;
     r = u0 + 0.5f * g;
+}
+
+// Error-free product of a float by a float pair (ch + cl): returns hi, adds
+// the rounding error and the low-part product to lo.
+__device__ __forceinline__ float two_prod_acc(float ch, float cl, float x, float& lo)
+{
+    const float p = ch * x;
+    lo += fmaf(ch, x, -p) + cl * x;
+    return p;
+}
+
+// Error-free sum of two floats: s + e == a + b exactly.
+__device__ __forceinline__ float two_sum(float a, float b, float& e)
+{
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return s;
 }
 
 // Error-free accumulation of a float into a (hi, lo) pair.
@@ -293,11 +312,15 @@ __device__ __forceinline__ void thinc_cand_f(const MixP& P, const float* sU, int
         float mn = (aR < aL) ? aR : aL;
         float mx = ((aL < aR) ? aR : aL) - mn;
         float theta = (float)((0.f < aR - aL) - (aR - aL < 0.f));
-        float C = (mx < 1e-20f) ? 0.f : (a0 - mn + 1e-20f) / (mx + 1e-20f);
-        bool mixed = (C > 1e-4f) && (C < (0.999999f - 1e-4f)) && ((aR - a0) * (a0 - aL) >= 0.f);
+        // C = (a0-mn+eps)/(mx+eps) (0 when mx < eps); the interval test is
+        // made on the numerator so that the division is only done when mixed
+        const float num = a0 - mn + 1e-20f, den = mx + 1e-20f;
+        bool mixed = !(mx < 1e-20f) && (num > 1e-4f * den) && (num < (0.999999f - 1e-4f) * den) &&
+                     ((aR - a0) * (a0 - aL) >= 0.f);
         c.L[m] = 0.f;
         c.R[m] = 0.f;
         if (mixed) {
+            const float C = num / den;
             c.mask |= 1u << m;
             float nx = -1.f / (8.f * P.dx[0]) *
                        (A[(ty + 1) * MP + tx + 1] + 2.f * A[ty * MP + tx + 1] + A[(ty - 1) * MP + tx + 1] -
@@ -345,10 +368,11 @@ __device__ void sweep_line(const MixP& P, const MixB& b, float* sm, int x0, int 
     Cand cd;
     cd.mask = 0;
     const bool valid = pos >= 0 && pos < n;
-    if (THINC) {
-        thinc_cand_f<M>(P, sU, tx, ty, D, cd);
+    if (THINC) thinc_cand_f<M>(P, sU, tx, ty, D, cd);
+    const bool flag = THINC && ((cd.mask >> (M - 1)) & 1u);
+    // the TBV comparison only runs in lines that hold a flagged cell
+    if (THINC && __any_sync(0xffffffffu, flag && valid && lane >= 1 && lane <= 30)) {
         unsigned mm = __shfl_up_sync(0xffffffffu, cd.mask, 1), mp = __shfl_down_sync(0xffffffffu, cd.mask, 1);
-        const bool flag = (cd.mask >> (M - 1)) & 1u;
         const int lo = valid ? b.bxlo[D][pos] : 0, hi = valid ? b.bxhi[D][pos] : -1;
         const bool in_m = valid && pos - 1 >= lo, in_p = valid && pos + 1 <= hi;
         const int cx = D == 0 ? pos : line, cy = D == 0 ? line : pos;
@@ -447,7 +471,7 @@ __device__ void sweep_line(const MixP& P, const MixB& b, float* sm, int x0, int 
     const int lo_bc = P.lo_bc[D], hi_bc = P.hi_bc[D];
     const int src = reflect_map(pos, n, lo_bc, hi_bc, refl);
     const int src_lane = src - p0;
-    {
+    if (p0 < 0 || p0 + 31 >= n) {  // only lines that reach the domain boundary
         const int sl = (src_lane >= 0 && src_lane < 32) ? src_lane : lane;
         FaceS<M>* S2[2] = {&SLs, &SRs};
 #pragma unroll
@@ -675,14 +699,27 @@ __global__ void __launch_bounds__(NTH, 2) k_stage2d(MixP P, MixB b, int stage)
             u[r] = ru[r] / rho;
             ke += 0.5f * rho * u[r] * u[r];
         }
-        double num = ((double)eh + (double)el) - (double)ke;
+        // p = (E - KE - sum e_cold + sum p_cold) / sum alpha/Gamma
+        // (boxaccesscellarray.cpp:116). The cold terms of a stiffened gas
+        // cancel E to four orders of magnitude, so the numerator is carried
+        // as an unevaluated float pair (error-free sums and products).
+        float sh = eh, sl = el, e, lo;
+        sh = two_sum(sh, -ke, e);
+        sl += e;
         float G = 0.f;
 #pragma unroll
         for (int m = 0; m < M; ++m) {
-            num = num - P.eE[m] * (double)ar[m] + P.cE[m] * (double)a[m];
+            lo = 0.f;
+            const float ec = two_prod_acc(P.eEh[m], P.eEl[m], ar[m], lo);
+            sh = two_sum(sh, -ec, e);
+            sl += e - lo;
+            lo = 0.f;
+            const float pc = two_prod_acc(P.cEh[m], P.cEl[m], a[m], lo);
+            sh = two_sum(sh, pc, e);
+            sl += e + lo;
             G += a[m] * P.ig[m];
         }
-        p = (float)num / G;
+        p = (sh + sl) / G;
         if (stage == 1) {
             // U1 = U*0.5 + U2*0.5 over the carried state (hllc.cpp:705)
 #pragma unroll
@@ -941,8 +978,11 @@ int mixed_alloc(MixedState& ms, const DevParams& DP, const std::vector<DevDomain
         P.ig[k] = (float)(1.0 / G);
         P.pref[k] = (float)DP.prm[k][1];
         P.eref[k] = (float)DP.prm[k][2];
-        P.cE[k] = DP.prm[k][1] / G;
-        P.eE[k] = DP.prm[k][2];
+        const double cE = DP.prm[k][1] / G, eE = DP.prm[k][2];
+        P.cEh[k] = (float)cE;
+        P.cEl[k] = (float)(cE - (double)P.cEh[k]);
+        P.eEh[k] = (float)eE;
+        P.eEl[k] = (float)(eE - (double)P.eEh[k]);
     }
     const long long N = ntot;
     const int NW = 3 * DP.M + 7;
