@@ -43,6 +43,18 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(ms: float, device: str = "cuda") -> float:
+    """Slowest rank's time (the job finishes when the last replica does)."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return ms
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def measured_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -158,13 +170,8 @@ def run_gpu_arm(args):
             ev1.record(stream)
         torch.cuda.synchronize()
     barrier()
-    ms = ev0.elapsed_time(ev1)
+    ms = max_over_ranks(ev0.elapsed_time(ev1))
     launches = g.launch_count() - l0
-    if ws > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
     clocks = clk.summary()
 
     # dominant kernel: per-launch time from the CUDA events around each launch
@@ -318,8 +325,8 @@ def run_reference_arm(args):
 
     port.build_port()
     nthr = port.threads()
-    # size the sample so that (warmup + steps) stays within about two minutes
-    budget = 120.0 / max(1, args.steps + args.warmup)
+    # size the sample so that (warmup + steps) stays within the time budget
+    budget = args.ref_budget / max(1, args.steps + args.warmup)
     n = 256
     probe = cases.shock_bubble_2d(n=n, max_grid_size=MAX_GRID // 4, max_steps=1)
     sim = port.PortSim(probe, omp=True)
@@ -359,6 +366,7 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ref-budget", type=float, default=120.0, help="seconds for the whole reference arm")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
