@@ -6,7 +6,7 @@ max_grid_size 128 (64 boxes), MUSCL + BVD-THINC (beta 1.6), CFL 0.4. One
 "step" is one full iteration of the reference's time loop (CFL reduction,
 two RK stages, RK2 average, cleanUpAlpha) over all cells.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--precision mixed|fp64]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--precision mixed|fp64|fused64]
     python bench.py --impl reference ...   # the CPU reference arm
 
 Prints one JSON line. `value` is cell-updates/s over the K timed steps
@@ -129,7 +129,7 @@ def run_gpu_arm(args):
     import torch
 
     from tenjin_gb300 import build, cases
-    from tenjin_gb300.host import FP64, MIXED, TenjinGPU
+    from tenjin_gb300.host import FP64, FUSED64, MIXED, TenjinGPU
 
     ws, rank, local = dist_env()
     torch.cuda.set_device(local)
@@ -137,7 +137,7 @@ def run_gpu_arm(args):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     build.build()
-    precision = MIXED if args.precision == "mixed" else FP64
+    precision = {"mixed": MIXED, "fp64": FP64, "fused64": FUSED64}[args.precision]
     case = cases.shock_bubble_2d(n=N_CELLS, max_grid_size=MAX_GRID, max_steps=1 << 30)
     ncell = case.total_cells
     g = TenjinGPU(case, precision)
@@ -175,8 +175,8 @@ def run_gpu_arm(args):
     clocks = clk.summary()
 
     # dominant kernel: per-launch time from the CUDA events around each launch
-    kernels = ["tj_stage_mixed", "tj_cfl_mixed"] if precision == MIXED else \
-        ["tj_recon_fp64", "tj_flux_fp64", "tj_update_fp64", "tj_cfl_fp64"]
+    kernels = {MIXED: ["tj_stage_mixed"], FUSED64: ["tj_stage_fused64"],
+               FP64: ["tj_recon_fp64", "tj_flux_fp64", "tj_update_fp64", "tj_cfl_fp64"]}[precision]
     ktimes = {}
     for k in kernels:
         tot, cnt = ctypes.c_double(), ctypes.c_longlong()
@@ -190,11 +190,11 @@ def run_gpu_arm(args):
     if dom:
         tot, cnt = ktimes[dom]
         per_launch_s = tot / cnt / 1e3
-        if precision == MIXED:
+        if precision in (MIXED, FUSED64):
             # algorithmic bytes of one stage launch: the carried state (12 words
-            # of 4 B) read and written once; stage 2 also reads U^n: 5 state
-            # passes per step spread over 2 launches
-            bytes_per_launch = 2.5 * 12 * 4 * ncell
+            # of 4 or 8 B) read and written once; stage 2 also reads U^n: 5
+            # state passes per step spread over 2 launches
+            bytes_per_launch = 2.5 * 12 * (4 if precision == MIXED else 8) * ncell
         else:
             bytes_per_launch = {"tj_recon_fp64": (7 + 2 * 14) * 8, "tj_flux_fp64": (2 * 14 + 9) * 8,
                                 "tj_update_fp64": (2 * 9 + 2 * 15) * 8, "tj_cfl_fp64": 10 * 8}[dom] * ncell
@@ -241,46 +241,31 @@ def run_gpu_arm(args):
                "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes, "steps": args.e2e_steps,
                "path": "tj_upload_domain + tj_step + tj_download_domain (AccessPattern layout, pinned host)"}
 
-    # FP32 vs FP64: the FP64 path on the same workload and step count (not
-    # part of the timed region): its throughput and the relative L1 error of
-    # the density field (sum of alphaRho) of the mixed result against it
-    fp64 = None
+    # accuracy and the FP64 speeds: the whole 2000-step workload (not part of
+    # the timed region) in the three precisions, each timed on its own stream
+    accuracy = None
     if precision == MIXED and args.fp64_compare:
-        M = case.M
-        dens32 = g.state(0)[M:2 * M].sum(axis=0)
-        g64 = TenjinGPU(case, FP64)
-        sp64 = ctypes.c_void_p()
-        lib.tj_get_stream(g64.h, ctypes.byref(sp64))
-        st64 = torch.cuda.ExternalStream(sp64.value)
-        g64.run(args.warmup + 1, 1e300)
-        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        with torch.cuda.stream(st64):
-            f0.record(st64)
-        g64.run(args.steps, 1e300)
-        with torch.cuda.stream(st64):
-            f1.record(st64)
-        torch.cuda.synchronize()
-        ms64 = f0.elapsed_time(f1)
-        dens64 = g64.state(0)[M:2 * M].sum(axis=0)
-        t32 = g.time()[0]
-        t64 = g64.time()[0]
-        g64.close()
-        fp64 = {"value": ncell * args.steps / (ms64 / 1e3), "unit": "cell-updates/s", "ms_per_step": ms64 / args.steps,
-                "l1_rel_density_err": float(abs(dens32 - dens64).sum() / abs(dens64).sum()),
-                "linf_rel_density_err": float(abs(dens32 - dens64).max() / abs(dens64).max()),
-                "steps_compared": args.warmup + 1 + args.steps, "t_mixed": t32, "t_fp64": t64}
+        accuracy = accuracy_runs(case, args.accuracy_steps)
+    # the second half of the metric: adjoint / forward time on the 2-D
+    # interface problem at 512^2, 200 steps, with a finite-difference check
+    configs = other_configs() if args.other_configs and rank == 0 else None
+    adjoint = None
+    if args.adjoint_dirs >= 0 and rank == 0:
+        from tenjin_gb300.adjoint import interface_problem_check
+        adjoint = interface_problem_check(512, 200, 20, args.adjoint_dirs)
     g.close()
     value = ncell * args.steps * ws / (ms / 1e3)
     line = {
         "metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32 (f64 closures)" if precision == MIXED else "f64",
+        "vs_baseline": None, "dtype": {MIXED: "f32 (compensated energy and pressure closure)", FUSED64: "f64 (fused kernels)",
+                                        FP64: "f64"}[precision],
         "data": "synthetic (seeded shock-bubble initial condition)",
         "config": {"workload": WORKLOAD, "cells": ncell, "precision": args.precision,
                    "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
                    "l2": "state working set larger than L2 (three state buffers of >= 48 MB plus scratch per step)"},
         "gpu_launches": launches, "steps_done": done, "e2e": e2e, "roofline": roofline, "clocks": clocks,
-        "fp64": fp64,
+        "accuracy": accuracy, "adjoint": adjoint, "other_configs": configs,
     }
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
@@ -289,6 +274,115 @@ def run_gpu_arm(args):
         dist.destroy_process_group()
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def _timed_run(g, steps):
+    """Device time (ms) of g.run(steps) on the context's stream."""
+    import torch
+
+    sp = ctypes.c_void_p()
+    g.L.tj_get_stream(g.h, ctypes.byref(sp))
+    st = torch.cuda.ExternalStream(sp.value)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    with torch.cuda.stream(st):
+        e0.record(st)
+    done, _ = g.run(steps, 1e300)
+    with torch.cuda.stream(st):
+        e1.record(st)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1), done
+
+
+def other_configs():
+    """The two 3-D configurations, measured beside the headline: the batch of
+    4096 uneven boxes (fused binary32 3-D kernel and the FP64 path, relative
+    L1 density error after 5 steps) and the copper plate at 256^3 (FP64
+    path: 5-wave solver, radial return, cleanUpV)."""
+    from tenjin_gb300 import cases
+    from tenjin_gb300.host import FP64, MIXED, TenjinGPU
+
+    out = {}
+    c = cases.uneven_boxes_3d()
+    g64 = TenjinGPU(c, FP64)
+    g64.run(2, 1e300)
+    ms64, d64 = _timed_run(g64, 3)
+    M = c.M
+    sample = range(0, len(c.domains), 8)
+    r64 = [g64.state(q)[M:2 * M].sum(axis=0) for q in sample]
+    g64.close()
+    g32 = TenjinGPU(c, MIXED)
+    g32.run(5, 1e300)
+    r32 = [g32.state(q)[M:2 * M].sum(axis=0) for q in sample]
+    import numpy as np
+    e = sum(float(np.abs(a - b).sum()) for a, b in zip(r32, r64)) / sum(float(np.abs(b).sum()) for b in r64)
+    g32.run(3, 1e300)
+    ms32, d32 = _timed_run(g32, 20)
+    buf = ctypes.create_string_buffer(256)
+    g32.L.tj_kernel_config(g32.h, buf, 256)
+    g32.close()
+    out["uneven_boxes_3d"] = {
+        "workload": f"{len(c.domains)} independent 3-D boxes, edges log-uniform in [8, 64], {c.total_cells} cells, "
+                    "water/air, MUSCL",
+        "mixed": {"value": c.total_cells * d32 / (ms32 / 1e3), "unit": "cell-updates/s", "steps": d32,
+                  "ms_per_step": ms32 / max(d32, 1), "kernel_config": buf.value.decode()},
+        "fp64": {"value": c.total_cells * d64 / (ms64 / 1e3), "unit": "cell-updates/s", "steps": d64,
+                 "ms_per_step": ms64 / max(d64, 1)},
+        "l1_rel_density_err_after_5_steps": e, "sampled_boxes": len(sample)}
+    c = cases.copper_plate_3d(n=256)
+    g = TenjinGPU(c, FP64)
+    g.run(1, 1e300)
+    ms, d = _timed_run(g, 2)
+    g.close()
+    out["copper_plate_3d"] = {
+        "workload": "copper plate impact, 256^3, Hugoniot Mie-Gruneisen, G 45 GPa, Y 90 MPa, plastic",
+        "fp64": {"value": c.total_cells * d / (ms / 1e3), "unit": "cell-updates/s", "steps": d,
+                 "ms_per_step": ms / max(d, 1)},
+        "mixed": "not built: the fused kernels cover fluids"}
+    return out
+
+
+def accuracy_runs(case, steps):
+    """The workload for `steps` steps from its initial state in binary32
+    (TJ_PRECISION_MIXED), in binary64 through the same fused kernels
+    (TJ_PRECISION_FUSED64) and through the reference-ordered FP64 kernels
+    (TJ_PRECISION_FP64): the relative L1 and Linf errors of the density field
+    (sum of alphaRho) between each pair, and each run's throughput."""
+    import torch
+
+    from tenjin_gb300.host import FP64, FUSED64, MIXED, TenjinGPU
+
+    M = case.M
+    dens, speed, tend = {}, {}, {}
+    for name, prec in (("mixed", MIXED), ("fused64", FUSED64), ("fp64", FP64)):
+        g = TenjinGPU(case, prec)
+        sp = ctypes.c_void_p()
+        g.L.tj_get_stream(g.h, ctypes.byref(sp))
+        st = torch.cuda.ExternalStream(sp.value)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        with torch.cuda.stream(st):
+            e0.record(st)
+        done, t = g.run(steps, 1e300)
+        with torch.cuda.stream(st):
+            e1.record(st)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        dens[name] = g.state(0)[M:2 * M].sum(axis=0)
+        speed[name] = {"value": case.total_cells * done / (ms / 1e3), "unit": "cell-updates/s",
+                       "ms_per_step": ms / max(done, 1)}
+        tend[name] = t
+        g.close()
+
+    def err(a, b):
+        e = abs(dens[a] - dens[b])
+        return {"l1_rel": float(e.sum() / abs(dens[b]).sum()), "linf_rel": float(e.max() / abs(dens[b]).max())}
+
+    return {"steps": steps, "field": "density (sum of alphaRho)",
+            "mixed_vs_fused64": err("mixed", "fused64"), "mixed_vs_fp64": err("mixed", "fp64"),
+            "fused64_vs_fp64": err("fused64", "fp64"), "t_end": tend, "throughput": speed,
+            "note": "fused64 and fp64 differ only by rounding; their difference is the FP64 round-off floor "
+                    "of this chaotic interface flow"}
 
 
 def cpu_baseline(target_seconds=15.0):
@@ -361,7 +455,12 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64", "fused64"])
+    ap.add_argument("--accuracy-steps", type=int, default=2000, help="steps of the precision comparison")
+    ap.add_argument("--no-other-configs", dest="other_configs", action="store_false",
+                    help="skip the 3-D configurations")
+    ap.add_argument("--adjoint-dirs", type=int, default=8,
+                    help="finite-difference directions of the adjoint check (-1: skip the adjoint)")
     ap.add_argument("--no-fp64-compare", dest="fp64_compare", action="store_false")
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)

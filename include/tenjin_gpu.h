@@ -55,8 +55,11 @@ extern "C" {
 #define TJ_BC_REFLECTIVE 1   /* reflect_even, reflect_odd for the normal velocity and momentum */
 
 #define TJ_PRECISION_FP64 0  /* every operation in binary64, reference order */
-#define TJ_PRECISION_MIXED 1 /* binary32 bulk; binary64 pressure closure, sound speed and
-                                conserved-state accumulation */
+#define TJ_PRECISION_MIXED 1 /* fused kernels in binary32 (2-D; 3-D fluids without THINC over
+                                any number of domains); total energy and the pressure-closure
+                                numerator as compensated pairs */
+#define TJ_PRECISION_FUSED64 2 /* the fused 2-D kernels in binary64: agrees with
+                                  TJ_PRECISION_FP64 to round-off, not bit for bit */
 
 typedef struct tj_material {
     int phase;        /* TJ_PHASE_* */
@@ -163,6 +166,34 @@ int tj_get_stream(tj_ctx* ctx, void** stream);
  * profiling was switched on. */
 int tj_set_profiling(tj_ctx* ctx, int on);
 int tj_kernel_time(tj_ctx* ctx, const char* kernel, double* ms_total, long long* launches);
+
+/* The launch configuration the fused kernels use (for 3-D: the tile shape
+ * the autotuner chose, the number of tiles and the persistent grid). No
+ * reference counterpart. */
+int tj_kernel_config(const tj_ctx* ctx, char* buf, unsigned long len);
+
+/* Adjoint pair (the forward / backward of a torch.autograd.Function). The
+ * reference has no adjoint; the pair differentiates its per-timestep update
+ * (main.cpp:145-170 with the loop of main.cpp:121-191) for 2-D fluids with
+ * the stiffened-gas EOS, one domain, TJ_PRECISION_FP64, dt frozen.
+ * tj_forward: initial state from the primitives prim0 (the tj_set_primitive
+ * layout) with the EOS parameters eos ([n_materials][TJ_MAX_EOS_PARAMS] in
+ * the getMaterialParameters order, initialise.cpp:125-235; NULL keeps the
+ * current ones), THINC scratch zeroed, then nsteps steps of advance +
+ * cleanUpAlpha with dt[n] (HOST array); the state and the THINC scratch are
+ * saved every `stride` steps. The final state is the context's state.
+ * tj_backward: from grad_state, the gradient of a scalar objective with
+ * respect to the final state (tj_download_domain layout; components derived
+ * from others - sound speed, sigma, USTAR - are ignored), to the gradient with
+ * respect to prim0 (grad_prim0, same layout as prim0) and to the EOS
+ * parameters (grad_eos, HOST, [n_materials][TJ_MAX_EOS_PARAMS]; nonzero for
+ * params 0-2). Each interval of `stride` steps is recomputed from its
+ * checkpoint and reversed; limiter, THINC and Riemann-solver branches are
+ * differentiated at their forward choice. prim0, grad_state and grad_prim0
+ * may be host or device pointers. */
+int tj_forward(tj_ctx* ctx, int domain, const double* prim0, const double* eos, int nsteps, const double* dt,
+               int stride);
+int tj_backward(tj_ctx* ctx, int domain, const double* grad_state, double* grad_prim0, double* grad_eos);
 
 /* Time step without any device allocation. No counterpart in the reference:
  * it exists for callers that cannot allocate device memory themselves (a

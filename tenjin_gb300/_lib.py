@@ -20,6 +20,7 @@ ERRORS = {
 }
 TJ_PRECISION_FP64 = 0
 TJ_PRECISION_MIXED = 1
+TJ_PRECISION_FUSED64 = 2
 
 
 class TjMaterial(ctypes.Structure):
@@ -78,6 +79,9 @@ SIGNATURES = [
     ("tj_set_profiling", _I, [_P, _I]),
     ("tj_kernel_time", _I, [_P, ctypes.c_char_p, _PD, ctypes.POINTER(ctypes.c_longlong)]),
     ("tj_compute_dt_noalloc", _I, [ctypes.POINTER(TjParams), _PI, _PD, ctypes.c_void_p, _PD, ctypes.c_void_p]),
+    ("tj_kernel_config", _I, [_P, ctypes.c_char_p, ctypes.c_ulong]),
+    ("tj_forward", _I, [_P, _I, ctypes.c_void_p, _PD, _I, _PD, _I]),
+    ("tj_backward", _I, [_P, _I, ctypes.c_void_p, ctypes.c_void_p, _PD]),
 ]
 
 _lib = None

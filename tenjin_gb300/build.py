@@ -27,7 +27,10 @@ UNITS = {
     # binary32 bulk: approximate division / square root, denormals flushed;
     # the compensated energy sum uses explicit round-to-nearest intrinsics
     "tj_mixed.cu": ["-use_fast_math"],
+    "tj_mixed3d.cu": ["-use_fast_math"],
     "tj_noalloc.cu": ["-fmad=false"],
+    # the adjoint's forward average must match the FP64 path bit for bit
+    "tj_adjoint.cu": ["-fmad=false"],
 }
 
 

@@ -180,9 +180,30 @@ def stiffened_shock_state(mach, rho1, p1, gamma, p_inf):
     return rho2, u2, p2
 
 
+def smooth_field(rng, n: int, modes: int = 4) -> np.ndarray:
+    """A seeded smooth field on an n x n grid: the mean of `modes` products of
+    sines with wavenumbers 1..4 and random phases and amplitudes (order 1)."""
+    x = (np.arange(n) + 0.5) / n
+    X, Y = np.meshgrid(x, x, indexing="xy")
+    f = np.zeros((n, n))
+    for _ in range(modes):
+        kx, ky = rng.integers(1, 5, 2)
+        f += rng.standard_normal() * np.sin(2 * np.pi * (kx * X + rng.uniform())) * \
+            np.sin(2 * np.pi * (ky * Y + rng.uniform()))
+    return f / modes
+
+
 def shock_bubble_2d(n: int = 1024, seed: int = 0, max_grid_size: int = 128, max_steps: int = 2000,
                     thinc: int = 1, cfl: float = 0.4, beta: float = 1.6, eps: float = 1e-6,
-                    radius: float = 0.2, shock_x: float = 0.2, mach: float = 1.5) -> Case:
+                    radius: float = 0.2, shock_x: float = 0.2, mach: float = 1.5,
+                    background: float = 0.0) -> Case:
+    """background > 0 multiplies rho_k (both materials) and p by 1 + background
+    * (a seeded smooth field), varies the air volume fraction by background *
+    field * alpha_air * alpha_water (so that both fractions stay in (0, 1)) and
+    adds 10 background m/s smooth fields to both velocity components: no
+    region of the initial state is then exactly uniform (the MUSCL limiter is
+    not differentiable at a uniform state; gradient checks need this
+    variant)."""
     mats = [Material(PHASE_FLUID, EOS_MIEGRUNEISEN, _stiffened(WATER_GAMMA, WATER_PINF)),
             Material(PHASE_FLUID, EOS_MIEGRUNEISEN, _stiffened(AIR_GAMMA, 0.0))]
     c = Case("shock_bubble_2d", 2, mats, thinc=thinc, cfl=cfl, thinc_beta=beta, max_steps=max_steps)
@@ -202,6 +223,15 @@ def shock_bubble_2d(n: int = 1024, seed: int = 0, max_grid_size: int = 128, max_
     prim[3, 0] = AIR_RHO
     prim[4, 0] = np.where(shocked, u2, 0.0)
     prim[7, 0] = np.where(shocked, p2, AMBIENT_P)
+    if background > 0.0:
+        for q in (2, 3, 7):
+            prim[q, 0] *= 1.0 + background * smooth_field(rng, n)
+        # volume fractions: a variation proportional to alpha_air alpha_water
+        # keeps both inside (0, 1)
+        a_air = prim[1, 0] + background * smooth_field(rng, n) * prim[1, 0] * prim[0, 0]
+        prim[1, 0], prim[0, 0] = a_air, 1.0 - a_air
+        prim[4, 0] += 10.0 * background * smooth_field(rng, n)
+        prim[5, 0] += 10.0 * background * smooth_field(rng, n)
     c.domains = [Domain(nn, [1.0, 1.0, 1.0], max_size_boxes(nn, 2, max_grid_size), prim)]
     return c
 

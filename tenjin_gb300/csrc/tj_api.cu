@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "tj_fp64.cuh"
+#include "tj_adjoint.cuh"
 #include "tj_mixed.cuh"
 #include "tj_types.h"
 
@@ -102,7 +103,11 @@ struct tj_ctx {
     std::vector<DevDomain> doms;
     std::vector<std::vector<int>> boxes;  // per domain, 6 ints per box
     long long ntot = 0, nftot[3] = {0, 0, 0};
-    bool geometry_dirty = true;
+    bool geometry_dirty = true;  // box table not yet on the device
+    // which copy of the state is current: the FP64 carried state A and/or the
+    // fused kernels' state (precisions MIXED / FUSED64); conversions are made
+    // when the other copy is next needed, not per call
+    bool a_current = true, x_current = true;
     // device memory
     DevDomain* d_doms = nullptr;
     int* d_boxes = nullptr;
@@ -119,6 +124,7 @@ struct tj_ctx {
     long long launches = 0;
     EventProf* prof = nullptr;
     long long graph_launches = 0;
+    AdjState* adj = nullptr;  // checkpoints and buffers of tj_forward / tj_backward
 };
 
 namespace {
@@ -144,6 +150,7 @@ void make_layouts(const tj_params& p, DevParams& P)
     P.thinc = p.THINC;
     P.plastic = p.PLASTIC;
     P.muscl = p.MUSCL;
+    P.fused64 = p.precision == TJ_PRECISION_FUSED64;
     for (int d = 0; d < 3; ++d) { P.lo_bc[d] = p.lo_bc[d]; P.hi_bc[d] = p.hi_bc[d]; }
     P.cfl = p.CFL;
     P.beta = p.THINCbeta;
@@ -260,6 +267,8 @@ void free_dev(tj_ctx* c)
     c->staging_bytes = 0;
     mixed_free(c->mixed);
     if (c->graph_exec) { cudaGraphExecDestroy(c->graph_exec); c->graph_exec = nullptr; }
+    adj_destroy(c->adj);
+    c->adj = nullptr;
 }
 
 Fp64Bufs bufs(tj_ctx* c)
@@ -273,11 +282,16 @@ Fp64Bufs bufs(tj_ctx* c)
     return b;
 }
 
-bool is_mixed(const tj_ctx* c) { return c->params.precision == TJ_PRECISION_MIXED; }
+// both fused precisions run the fused kernels
+bool is_mixed(const tj_ctx* c)
+{
+    return c->params.precision == TJ_PRECISION_MIXED || c->params.precision == TJ_PRECISION_FUSED64;
+}
 
 // Upload the box table and the cell -> box map (geometry changes only).
 int sync_boxes(tj_ctx* c)
 {
+    c->geometry_dirty = false;
     std::vector<int> flat;
     std::vector<int> cell_box(c->ntot);
     for (size_t q = 0; q < c->doms.size(); ++q) {
@@ -306,7 +320,40 @@ int sync_boxes(tj_ctx* c)
 int need_state(tj_ctx* c)
 {
     if (c->doms.empty() || !c->A) return fail(c, TJ_ERR_STATE, "no domain set (tj_set_domains)");
+    if (c->geometry_dirty) {
+        TJ_CUDA(c, cudaStreamSynchronize(c->stream));
+        int e = sync_boxes(c);
+        if (e) return e;
+    }
     return TJ_OK;
+}
+
+// The FP64 carried state is about to be read: bring it up to date.
+void a_sync(tj_ctx* c)
+{
+    if (is_mixed(c) && !c->a_current) {
+        Fp64Bufs b = bufs(c);
+        c->launches += mixed_to_fp64(c->mixed, c->P, b, c->stream);
+        c->a_current = true;
+    }
+}
+
+// The fused kernels are about to run: bring their state up to date (and arm
+// the CFL minimum of the next step).
+void x_sync(tj_ctx* c)
+{
+    if (is_mixed(c) && !c->x_current) {
+        Fp64Bufs b = bufs(c);
+        c->launches += mixed_from_fp64(c->mixed, c->P, b, c->stream);
+        c->x_current = true;
+    }
+}
+
+// The FP64 carried state was written.
+void a_written(tj_ctx* c)
+{
+    c->a_current = true;
+    if (is_mixed(c)) c->x_current = false;
 }
 
 int check_status(tj_ctx* c)
@@ -381,8 +428,11 @@ int tj_create(const tj_params* p, tj_ctx** out)
         }
     }
     if (p->SOLID && !any_solid) return bad("SOLID needs a solid material");
-    if (p->precision != TJ_PRECISION_FP64 && p->precision != TJ_PRECISION_MIXED) return bad("unknown precision");
-    if (p->precision == TJ_PRECISION_MIXED && !mixed_supported(*p)) return bad("mixed precision supports fluids only");
+    if (p->precision != TJ_PRECISION_FP64 && p->precision != TJ_PRECISION_MIXED && p->precision != TJ_PRECISION_FUSED64)
+        return bad("unknown precision");
+    if (p->precision != TJ_PRECISION_FP64 && !mixed_supported(*p))
+        return bad("the fused precisions support fluids with the stiffened-gas EOS in 2-D, and in 3-D without THINC "
+                   "in binary32 only");
     make_layouts(*p, c->P);
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return bad("no CUDA device");
     if (cudaMalloc(&c->d_scal, sizeof(DevScalars)) != cudaSuccess) return bad("cudaMalloc failed");
@@ -476,6 +526,7 @@ int tj_set_domains(tj_ctx* c, int nd, const int* n_cells, const double* dim_l)
             }
         }
     }
+    c->a_current = c->x_current = true;  // both copies start zero
     int e = sync_boxes(c);
     if (e) return e;
     return tj_set_time(c, 0.0, 0);
@@ -497,8 +548,8 @@ int tj_set_boxes(tj_ctx* c, int q, int nbox, const int* lohi)
     for (int v : cover)
         if (v != 1) return fail(c, TJ_ERR_ARG, "boxes must tile the domain exactly once");
     c->boxes[q].assign(lohi, lohi + 6 * nbox);
-    TJ_CUDA(c, cudaStreamSynchronize(c->stream));
-    return sync_boxes(c);
+    c->geometry_dirty = true;  // uploaded before the next operation that needs it
+    return TJ_OK;
 }
 
 int tj_set_max_grid_size(tj_ctx* c, int q, int mgs)
@@ -552,16 +603,16 @@ static int exchange(tj_ctx* c, int q, const int* bx, double* host, int ncomp, in
     e = ensure_staging(c, bytes);
     if (e) return e;
     Fp64Bufs b = bufs(c);
+    a_sync(c);  // the cells outside this box keep their current values
     if (up) {
-        TJ_CUDA(c, cudaMemcpyAsync(c->staging, host, bytes, cudaMemcpyHostToDevice, c->stream));
+        TJ_CUDA(c, cudaMemcpyAsync(c->staging, host, bytes, cudaMemcpyDefault, c->stream));
         c->launches += fp64_ap_to_state(c->P, b, q, bx, c->staging, ld_i, ld_j, ld_k, cs, ngrow, c->A, c->stream);
-        if (is_mixed(c)) c->launches += mixed_from_fp64(c->mixed, c->P, b, c->stream);
+        a_written(c);
         TJ_CUDA(c, cudaStreamSynchronize(c->stream));
     } else {
-        if (is_mixed(c)) c->launches += mixed_to_fp64(c->mixed, c->P, b, c->stream);
-        if (ngrow > 0) TJ_CUDA(c, cudaMemcpyAsync(c->staging, host, bytes, cudaMemcpyHostToDevice, c->stream));
+        if (ngrow > 0) TJ_CUDA(c, cudaMemcpyAsync(c->staging, host, bytes, cudaMemcpyDefault, c->stream));
         c->launches += fp64_state_to_ap(c->P, b, q, bx, c->A, c->staging, ld_i, ld_j, ld_k, cs, ngrow, c->stream);
-        TJ_CUDA(c, cudaMemcpyAsync(host, c->staging, bytes, cudaMemcpyDeviceToHost, c->stream));
+        TJ_CUDA(c, cudaMemcpyAsync(host, c->staging, bytes, cudaMemcpyDefault, c->stream));
         TJ_CUDA(c, cudaStreamSynchronize(c->stream));
     }
     TJ_CUDA(c, cudaGetLastError());
@@ -608,10 +659,11 @@ int tj_set_primitive(tj_ctx* c, int q, const double* prim)
     size_t bytes = sizeof(double) * nprim * (size_t)D.n[0] * D.n[1] * D.n[2];
     e = ensure_staging(c, bytes);
     if (e) return e;
-    TJ_CUDA(c, cudaMemcpyAsync(c->staging, prim, bytes, cudaMemcpyHostToDevice, c->stream));
+    TJ_CUDA(c, cudaMemcpyAsync(c->staging, prim, bytes, cudaMemcpyDefault, c->stream));
+    a_sync(c);
     Fp64Bufs b = bufs(c);
     c->launches += fp64_prim_to_state(c->P, b, q, c->staging, c->A, c->stream);
-    if (is_mixed(c)) c->launches += mixed_from_fp64(c->mixed, c->P, b, c->stream);
+    a_written(c);
     TJ_CUDA(c, cudaStreamSynchronize(c->stream));
     TJ_CUDA(c, cudaGetLastError());
     return TJ_OK;
@@ -625,6 +677,7 @@ int tj_compute_dt(tj_ctx* c, double* dt)
     Fp64Bufs b = bufs(c);
     c->launches += fp64_set_dt(b, 0.0, c->stream);
     if (is_mixed(c)) {
+        x_sync(c);
         c->launches += mixed_compute_dt(c->mixed, c->P, b, c->stream);
         c->launches += fp64_dt_finalize(c->P, b, 0, c->stream);
         c->launches += mixed_compute_dt(c->mixed, c->P, b, c->stream);  // re-arm for the next step
@@ -660,9 +713,9 @@ static int cell_op(tj_ctx* c, int op)
     int e = need_state(c);
     if (e) return e;
     Fp64Bufs b = bufs(c);
-    if (is_mixed(c)) c->launches += mixed_to_fp64(c->mixed, c->P, b, c->stream);
+    a_sync(c);
     c->launches += fp64_cell_op(c->P, b, c->A, nullptr, op, c->stream);
-    if (is_mixed(c) && op != OP_NAN) c->launches += mixed_from_fp64(c->mixed, c->P, b, c->stream);
+    if (op != OP_NAN) a_written(c);
     TJ_CUDA(c, cudaGetLastError());
     return check_status(c);
 }
@@ -686,7 +739,7 @@ int tj_contains_nan(tj_ctx* c, int* flag)
     if (e) return e;
     TJ_CUDA(c, cudaMemsetAsync(&c->d_scal->nan_flag, 0, sizeof(int), c->stream));
     Fp64Bufs b = bufs(c);
-    if (is_mixed(c)) c->launches += mixed_to_fp64(c->mixed, c->P, b, c->stream);
+    a_sync(c);
     c->launches += fp64_cell_op(c->P, b, c->A, nullptr, OP_NAN, c->stream);
     DevScalars s;
     TJ_CUDA(c, cudaMemcpyAsync(&s, c->d_scal, sizeof s, cudaMemcpyDeviceToHost, c->stream));
@@ -740,7 +793,9 @@ int tj_step(tj_ctx* c, double t_end)
     if (e) return e;
     e = set_t_end(c, t_end);
     if (e) return e;
+    x_sync(c);
     issue_step(c);
+    if (is_mixed(c)) c->a_current = false;
     TJ_CUDA(c, cudaGetLastError());
     return TJ_OK;
 }
@@ -756,6 +811,8 @@ int tj_run(tj_ctx* c, int nsteps, double t_end, int* steps_done, double* t_out)
     double t0 = 0;
     e = tj_get_time(c, &t0, &n0, nullptr);
     if (e) return e;
+    x_sync(c);  // outside any capture
+    if (is_mixed(c) && nsteps > 0) c->a_current = false;
     const int group = 20;
     long long per_group = 0;
     if (!c->graph_exec || c->graph_steps != group) {
@@ -837,6 +894,87 @@ int tj_get_stream(tj_ctx* c, void** stream)
 {
     if (!c || !stream) return TJ_ERR_ARG;
     *stream = (void*)c->stream;
+    return TJ_OK;
+}
+
+int tj_forward(tj_ctx* c, int q, const double* prim0, const double* eos, int nsteps, const double* dt, int stride)
+{
+    if (!c || !prim0 || !dt || nsteps < 1 || stride < 1) return fail(c, TJ_ERR_ARG, "bad tj_forward arguments");
+    int e = need_state(c);
+    if (e) return e;
+    if (q != 0) return fail(c, TJ_ERR_ARG, "tj_forward: domain 0 only");
+    if (c->params.precision != TJ_PRECISION_FP64) return fail(c, TJ_ERR_ARG, "tj_forward runs the FP64 path");
+    const char* why = adj_unsupported(c->P, (int)c->doms.size());
+    if (why) return fail(c, TJ_ERR_ARG, why);
+    for (int n = 0; n < nsteps; ++n)
+        if (!(dt[n] > 0.0)) return fail(c, TJ_ERR_ARG, "tj_forward: dt must be positive");
+    if (eos)
+        for (int m = 0; m < c->P.M; ++m)
+            for (int k = 0; k < c->params.materials[m].nparams && k < TJ_MAX_EOS_PARAMS; ++k) {
+                c->P.prm[m][k] = eos[m * TJ_MAX_EOS_PARAMS + k];
+                c->params.materials[m].params[k] = eos[m * TJ_MAX_EOS_PARAMS + k];
+            }
+    const DevDomain& D = c->doms[0];
+    const size_t nprim = 2 * c->P.M + 4;
+    const size_t bytes = sizeof(double) * nprim * (size_t)c->ntot;
+    e = ensure_staging(c, bytes);
+    if (e) return e;
+    TJ_CUDA(c, cudaMemcpyAsync(c->staging, prim0, bytes, cudaMemcpyDefault, c->stream));
+    // a fresh start: THINC scratch zero, as after the reference's allocation
+    if (c->ulstar) {
+        TJ_CUDA(c, cudaMemsetAsync(c->ulstar, 0, sizeof(double) * c->P.M * c->ntot, c->stream));
+        TJ_CUDA(c, cudaMemsetAsync(c->urstar, 0, sizeof(double) * c->P.M * c->ntot, c->stream));
+        for (int d = 0; d < 3; ++d)
+            if (c->gstar[d])
+                TJ_CUDA(c, cudaMemsetAsync(c->gstar[d], 0, sizeof(double) * c->P.M * c->nftot[d], c->stream));
+    }
+    Fp64Bufs b = bufs(c);
+    c->launches += fp64_prim_to_state(c->P, b, 0, c->staging, c->A, c->stream);
+    if (!c->adj) c->adj = adj_create();
+    long long n = adj_forward(c->adj, c->P, b, D, dt, nsteps, stride, c->stream);
+    if (n < 0) return fail(c, (int)n, "tj_forward: device allocation failed");
+    c->launches += n;
+    TJ_CUDA(c, cudaGetLastError());
+    e = check_status(c);
+    if (e) return e;
+    double t = 0.0;
+    for (int k = 0; k < nsteps; ++k) t += dt[k];
+    return tj_set_time(c, t, nsteps);
+}
+
+int tj_backward(tj_ctx* c, int q, const double* grad_state, double* grad_prim0, double* grad_eos)
+{
+    if (!c || !grad_state || !grad_prim0 || !grad_eos) return fail(c, TJ_ERR_ARG, "bad tj_backward arguments");
+    int e = need_state(c);
+    if (e) return e;
+    if (q != 0) return fail(c, TJ_ERR_ARG, "tj_backward: domain 0 only");
+    if (!c->adj) return fail(c, TJ_ERR_STATE, "tj_backward needs a tj_forward first");
+    const DevDomain& D = c->doms[0];
+    const int nx = D.n[0], ny = D.n[1];
+    const long long N = c->ntot;
+    const size_t in_bytes = sizeof(double) * c->P.NCOMP * (size_t)N;
+    const size_t out_bytes = sizeof(double) * (2 * c->P.M + 4) * (size_t)N;
+    e = ensure_staging(c, std::max(in_bytes, out_bytes));
+    if (e) return e;
+    TJ_CUDA(c, cudaMemcpyAsync(c->staging, grad_state, in_bytes, cudaMemcpyDefault, c->stream));
+    Fp64Bufs b = bufs(c);
+    // the adjoint of the final state in the carried layout, in C (unused by the recompute)
+    int bx[6] = {0, 0, 0, nx - 1, ny - 1, 0};
+    c->launches += fp64_ap_to_state(c->P, b, 0, bx, c->staging, nx, ny, 1, N, 0, c->C, c->stream);
+    long long n = adj_backward(c->adj, c->P, b, D, c->C, c->staging, grad_eos, c->stream);
+    if (n < 0) return fail(c, (int)n, "tj_backward: no forward to reverse");
+    c->launches += n;
+    TJ_CUDA(c, cudaMemcpyAsync(grad_prim0, c->staging, out_bytes, cudaMemcpyDefault, c->stream));
+    TJ_CUDA(c, cudaStreamSynchronize(c->stream));
+    TJ_CUDA(c, cudaGetLastError());
+    return check_status(c);
+}
+
+int tj_kernel_config(const tj_ctx* c, char* buf, unsigned long len)
+{
+    if (!c || !buf || len == 0) return TJ_ERR_ARG;
+    if (is_mixed(c)) mixed_describe(c->mixed, buf, len);
+    else std::snprintf(buf, len, "fp64 per-direction kernels");
     return TJ_OK;
 }
 

@@ -339,6 +339,7 @@ __global__ void k_recon(DevParams P, Fp64Bufs b, const double* __restrict__ X, i
             if (in_p) thinc_cand(P, D, X, nt, i + o[0], j + o[1], k + o[2], d, tp);
             const long long gmm = D.off + (i - o[0]) + (long long)D.n[0] * ((j - o[1]) + (long long)D.n[1] * (k - o[2]));
             const long long gpp = D.off + (i + o[0]) + (long long)D.n[0] * ((j + o[1]) + (long long)D.n[1] * (k + o[2]));
+            int code = 0;
             for (int m = 0; m < P.M; ++m) {
                 const int a = P.S_ALPHA + m;
                 double urm, ulp, trm, tlp;
@@ -376,7 +377,15 @@ __global__ void k_recon(DevParams P, Fp64Bufs b, const double* __restrict__ X, i
                 if (tc.flag && tbvt < tbvm) {
                     L.alpha[m] = tpl;
                     R.alpha[m] = tpr;
+                    code |= (tc.mixed[m] ? 1 : 2) << (2 * m);
                 }
+            }
+            if (b.rec) {
+                for (int m = 0; m < P.M; ++m) {
+                    b.rec[((long long)(d * 2) * P.M + m) * nt + g] = L.alpha[m];
+                    b.rec[((long long)(d * 2 + 1) * P.M + m) * nt + g] = R.alpha[m];
+                }
+                b.rec_code[(long long)d * nt + g] = code;
             }
             // THINC pass 1 writes its candidates into the persistent scratch.
             for (int m = 0; m < P.M; ++m)

@@ -17,6 +17,13 @@ struct Fp64Bufs {
     DevScalars* scal;
     long long ntot, nftot[3];
     int ndom;
+    // optional record of the reconstruction (for the adjoint's recompute):
+    // alpha of UL and UR after the BVD choice, before cleanUpAlpha, at
+    // rec[((d * 2 + side) * M + m) * ntot + g], and per cell and direction
+    // 2 bits per material at rec_code[d * ntot + g]: 0 MUSCL, 1 the cell's
+    // own THINC candidate, 2 a value of the THINC scratch
+    double* rec = nullptr;
+    int* rec_code = nullptr;
 };
 
 // Launch helpers (tj_fp64.cu). Each returns the number of kernel launches.

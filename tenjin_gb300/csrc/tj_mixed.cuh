@@ -1,4 +1,5 @@
-// Mixed-precision (binary32 bulk) fused kernels of the per-timestep update.
+// Fused stage kernels of the per-timestep update: 2-D (binary32 or binary64
+// working type) and 3-D over many domains (binary32).
 #pragma once
 
 #include <vector>
@@ -12,6 +13,26 @@ struct MixedState {
     bool allocated = false;
     void* impl = nullptr;
 };
+
+// One fused implementation (2-D single domain; 3-D many domains).
+struct MixedBase {
+    virtual ~MixedBase() {}
+    virtual int set_boxes(const std::vector<DevDomain>& doms, const std::vector<std::vector<int>>& boxes,
+                          cudaStream_t st) = 0;
+    virtual int from_fp64(const DevParams& DP, const Fp64Bufs& fb, cudaStream_t st) = 0;
+    virtual int to_fp64(const DevParams& DP, const Fp64Bufs& fb, cudaStream_t st) = 0;
+    virtual int cfl(const Fp64Bufs& fb, cudaStream_t st) = 0;
+    virtual int step(const DevParams& DP, const Fp64Bufs& fb, cudaStream_t st, Prof* pr) = 0;
+    // a one-line description of the launch configuration in use
+    virtual void describe(char* buf, size_t len) const
+    {
+        if (len) buf[0] = 0;
+    }
+};
+
+// The 3-D fluid implementation (tj_mixed3d.cu).
+MixedBase* mixed3d_create(const DevParams& DP, const std::vector<DevDomain>& doms, long long ntot, cudaStream_t st,
+                          int* err);
 
 bool mixed_supported(const tj_params& p);
 int mixed_alloc(MixedState& m, const DevParams& P, const std::vector<DevDomain>& doms, long long ntot,
@@ -27,5 +48,6 @@ int mixed_to_fp64(MixedState& m, const DevParams& P, const Fp64Bufs& b, cudaStre
 int mixed_compute_dt(MixedState& m, const DevParams& P, const Fp64Bufs& b, cudaStream_t st);
 int mixed_step(MixedState& m, const DevParams& P, const Fp64Bufs& b, cudaStream_t st, Prof* pr = nullptr);
 int mixed_launches_per_step(const DevParams& P);
+void mixed_describe(const MixedState& m, char* buf, size_t len);
 
 }  // namespace tj

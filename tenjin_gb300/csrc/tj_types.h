@@ -11,6 +11,7 @@ namespace tj {
 // arrays (component offsets). Passed to kernels by value.
 struct DevParams {
     int dim, M, solid, thinc, plastic, muscl, any_solid;
+    int fused64;  // fused kernels in binary64 (TJ_PRECISION_FUSED64)
     int lo_bc[3], hi_bc[3];
     double cfl, beta;
     int phase[TJ_MAX_MAT], eos[TJ_MAX_MAT];

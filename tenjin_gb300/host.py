@@ -32,6 +32,7 @@ from .cases import Case
 
 FP64 = _lib.TJ_PRECISION_FP64
 MIXED = _lib.TJ_PRECISION_MIXED
+FUSED64 = _lib.TJ_PRECISION_FUSED64
 
 
 def _dp(a: np.ndarray):

@@ -1,12 +1,15 @@
-"""Mixed-precision path (binary32 bulk, compensated energy, binary64 pressure
-closure) against the FP64 reference-faithful path on the same inputs. The
-stated bound is the relative L1 error of the density field (sum of
-alphaRho): <= 1e-4."""
+"""Fused 2-D kernels in binary32 (TJ_PRECISION_MIXED: compensated energy and
+pressure closure) and in binary64 (TJ_PRECISION_FUSED64) against the
+reference-ordered FP64 path on the same inputs. The stated bound is the
+relative L1 error of the density field (sum of alphaRho): <= 1e-4. The
+binary64 instance of the fused kernels differs from the FP64 path by rounding
+only, which the tests pin while the flow is still smooth (before the shock
+reaches the bubble)."""
 import numpy as np
 import pytest
 
 from tenjin_gb300 import build, cases
-from tenjin_gb300.host import FP64, MIXED, TenjinGPU
+from tenjin_gb300.host import FP64, FUSED64, MIXED, TenjinGPU
 
 pytestmark = pytest.mark.gpu
 L1_TOL = 1e-4
@@ -61,3 +64,25 @@ def test_mixed_reflective_walls_run():
     d32, _, s32 = run(c, MIXED, 30)
     r64, r32 = density(s64, c.M), density(s32, c.M)
     assert np.abs(r32 - r64).sum() / np.abs(r64).sum() <= L1_TOL
+
+
+@pytest.mark.parametrize("thinc", [1, 0])
+def test_fused64_agrees_with_fp64_to_roundoff(thinc):
+    # 20 steps at 128^2: the shock has not reached the bubble yet
+    c = cases.shock_bubble_2d(n=128, max_grid_size=64, max_steps=20, thinc=thinc)
+    d64, t64, s64 = run(c, FP64, 20)
+    dfu, tfu, sfu = run(c, FUSED64, 20)
+    assert d64 == dfu == 20
+    assert abs(tfu - t64) <= 1e-13 * t64
+    r64, rfu = density(s64, c.M), density(sfu, c.M)
+    assert np.abs(rfu - r64).sum() / np.abs(r64).sum() <= 1e-13
+    assert np.abs(rfu - r64).max() / np.abs(r64).max() <= 1e-11
+
+
+def test_mixed_against_fused64_through_the_interface():
+    # 60 steps at 128^2: the shock crosses the bubble interface
+    c = cases.shock_bubble_2d(n=128, max_grid_size=64, max_steps=60, thinc=1)
+    _, _, sfu = run(c, FUSED64, 60)
+    _, _, s32 = run(c, MIXED, 60)
+    rfu, r32 = density(sfu, c.M), density(s32, c.M)
+    assert np.abs(r32 - rfu).sum() / np.abs(rfu).sum() <= L1_TOL
