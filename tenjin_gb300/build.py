@@ -28,6 +28,9 @@ UNITS = {
     # the compensated energy sum uses explicit round-to-nearest intrinsics
     "tj_mixed.cu": ["-use_fast_math"],
     "tj_mixed3d.cu": ["-use_fast_math"],
+    # binary32 general path: fast binary32 arithmetic; its binary64 closure and
+    # yield projection need no bit-exactness
+    "tj_fp32.cu": ["-use_fast_math"],
     "tj_noalloc.cu": ["-fmad=false"],
     # the adjoint's forward average must match the FP64 path bit for bit
     "tj_adjoint.cu": ["-fmad=false"],

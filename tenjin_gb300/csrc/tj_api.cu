@@ -151,6 +151,7 @@ void make_layouts(const tj_params& p, DevParams& P)
     P.plastic = p.PLASTIC;
     P.muscl = p.MUSCL;
     P.fused64 = p.precision == TJ_PRECISION_FUSED64;
+    P.S_ELO = -1;
     for (int d = 0; d < 3; ++d) { P.lo_bc[d] = p.lo_bc[d]; P.hi_bc[d] = p.hi_bc[d]; }
     P.cfl = p.CFL;
     P.beta = p.THINCbeta;

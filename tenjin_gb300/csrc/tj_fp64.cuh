@@ -5,12 +5,13 @@
 
 namespace tj {
 
-struct Fp64Bufs {
-    double *A, *B, *C;        // state: U^n (and result), stage-1 output, stage-2 partial
-    double *UL, *UR;          // reconstructed face states, one per cell
-    double* FX;               // face fluxes of the current direction
-    double *ulstar, *urstar;  // THINC scratch (alpha of the reference's ULStar / URStar)
-    double* gstar[3];         // ULStar ghost alpha at box hi+1 faces, per direction
+template <typename R>
+struct PathBufs {
+    R *A, *B, *C;        // state: U^n (and result), stage-1 output, stage-2 partial
+    R *UL, *UR;          // reconstructed face states, one per cell
+    R* FX;               // face fluxes of the current direction
+    R *ulstar, *urstar;  // THINC scratch (alpha of the reference's ULStar / URStar)
+    R* gstar[3];         // ULStar ghost alpha at box hi+1 faces, per direction
     int* cell_box;            // domain-local box index of each cell
     int* boxes;               // 6 ints per box, all domains
     DevDomain* doms;
@@ -22,9 +23,13 @@ struct Fp64Bufs {
     // rec[((d * 2 + side) * M + m) * ntot + g], and per cell and direction
     // 2 bits per material at rec_code[d * ntot + g]: 0 MUSCL, 1 the cell's
     // own THINC candidate, 2 a value of the THINC scratch
-    double* rec = nullptr;
+    R* rec = nullptr;
     int* rec_code = nullptr;
 };
+using Fp64Bufs = PathBufs<double>;
+
+// The binary32 parameter block of a binary64 one (tj_fp32.cu).
+DevParams32 make_params32(const DevParams& P);
 
 // Launch helpers (tj_fp64.cu). Each returns the number of kernel launches.
 int fp64_cfl(const DevParams& P, const Fp64Bufs& b, const double* X, cudaStream_t st, Prof* pr = nullptr);

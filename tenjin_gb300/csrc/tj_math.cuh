@@ -132,4 +132,12 @@ __device__ inline double tjm_tanh(double x)
     return copysign(r, x);
 }
 
+// binary32 overloads (the binary32 instance of the kernels; fast-math library calls)
+__device__ inline float tjm_exp(float x) { return expf(x); }
+__device__ inline float tjm_expm1(float x) { return expm1f(x); }
+__device__ inline float tjm_log(float x) { return logf(x); }
+__device__ inline float tjm_pow(float x, float y) { return powf(x, y); }
+__device__ inline float tjm_cosh(float x) { return coshf(x); }
+__device__ inline float tjm_tanh(float x) { return tanhf(x); }
+
 }  // namespace tj

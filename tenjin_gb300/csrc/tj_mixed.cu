@@ -82,6 +82,7 @@ struct MixP {
     int nx, ny, M, thinc;
     int lo_bc[2], hi_bc[2];
     R dx[2], idx[2], beta;
+    R mxfloor;  // smallest alpha variation the THINC mixed-cell test accepts (thinc.cpp:86-87: 1e-20)
     R g[TJ_MAX_MAT], ig[TJ_MAX_MAT], pref[TJ_MAX_MAT], eref[TJ_MAX_MAT];
     // pref/Gamma and eref as pairs (hi + lo) for the pressure closure
     R cEh[TJ_MAX_MAT], cEl[TJ_MAX_MAT], eEh[TJ_MAX_MAT], eEl[TJ_MAX_MAT];
@@ -353,7 +354,7 @@ __device__ __forceinline__ void thinc_cand_f(const MixP<R>& P, const R* sU, int 
         // C = (a0-mn+eps)/(mx+eps) (0 when mx < eps); the interval test is
         // made on the numerator so that the division is only done when mixed
         const R num = a0 - mn + R(1e-20), den = mx + R(1e-20);
-        const bool mixed = !(mx < R(1e-20)) && (num > R(1e-4) * den) && (num < (R(0.999999) - R(1e-4)) * den) &&
+        const bool mixed = !(mx < P.mxfloor) && (num > R(1e-4) * den) && (num < (R(0.999999) - R(1e-4)) * den) &&
                            ((aR - a0) * (a0 - aL) >= R(0));
         c.L[m] = R(0);
         c.Rr[m] = R(0);
@@ -999,6 +1000,7 @@ struct MixedImpl : MixedBase {
             P.dxd[d] = D.dx[d];
         }
         P.beta = (R)DP.beta;
+        P.mxfloor = (R)1e-20;
         for (int k = 0; k < DP.M; ++k) {
             const double G = DP.prm[k][0] - 1.0;
             P.g[k] = (R)G;
@@ -1181,11 +1183,30 @@ struct MixedImpl : MixedBase {
 
 }  // namespace
 
+// The fused 2-D kernels: one 2-D fluid domain with the stiffened-gas EOS.
+static bool fused2d_covers(const DevParams& DP, size_t ndom)
+{
+    if (DP.dim != 2 || DP.solid || DP.plastic || ndom != 1 || DP.M > 4) return false;
+    for (int m = 0; m < DP.M; ++m)
+        if (DP.eos[m] != TJ_EOS_MIEGRUNEISEN || DP.phase[m] != TJ_PHASE_FLUID) return false;
+    return true;
+}
+
+// The fused 3-D kernel: 3-D fluids with the stiffened-gas EOS, MUSCL (no THINC).
+static bool fused3d_covers(const DevParams& DP)
+{
+    if (DP.dim != 3 || DP.solid || DP.plastic || DP.thinc || DP.M > 4) return false;
+    for (int m = 0; m < DP.M; ++m)
+        if (DP.eos[m] != TJ_EOS_MIEGRUNEISEN || DP.phase[m] != TJ_PHASE_FLUID) return false;
+    return true;
+}
+
 bool mixed_supported(const tj_params& p)
 {
-    if (p.SOLID || p.PLASTIC || p.THINC && p.dim != 2) return false;
-    if (p.dim == 3 && p.precision == TJ_PRECISION_FUSED64) return false;  // 3-D: binary32 only
-    if (p.dim != 2 && p.dim != 3) return false;
+    // binary32: every configuration (fused kernels where they apply, the
+    // binary32 per-direction kernels otherwise); binary64 fused: 2-D fluids
+    if (p.precision == TJ_PRECISION_MIXED) return true;
+    if (p.dim != 2 || p.SOLID || p.PLASTIC) return false;
     if (p.n_materials < 1 || p.n_materials > 4) return false;
     for (int m = 0; m < p.n_materials; ++m)
         if (p.materials[m].eos != TJ_EOS_MIEGRUNEISEN || p.materials[m].phase != TJ_PHASE_FLUID) return false;
@@ -1195,10 +1216,15 @@ bool mixed_supported(const tj_params& p)
 int mixed_alloc(MixedState& ms, const DevParams& DP, const std::vector<DevDomain>& doms, long long ntot,
                 const long long* nftot, cudaStream_t st)
 {
-    (void)nftot;
-    if (DP.dim == 3) {
+    if (!DP.fused64 && fused3d_covers(DP)) {
         int err = TJ_OK;
         ms.impl = mixed3d_create(DP, doms, ntot, st, &err);
+        ms.allocated = true;
+        return err;
+    }
+    if (!DP.fused64 && !fused2d_covers(DP, doms.size())) {
+        int err = TJ_OK;
+        ms.impl = general32_create(DP, ntot, nftot, st, &err);
         ms.allocated = true;
         return err;
     }

@@ -30,6 +30,9 @@ struct MixedBase {
     }
 };
 
+// The binary32 per-direction kernels for every other configuration (tj_fp32.cu).
+MixedBase* general32_create(const DevParams& DP, long long ntot, const long long* nftot, cudaStream_t st, int* err);
+
 // The 3-D fluid implementation (tj_mixed3d.cu).
 MixedBase* mixed3d_create(const DevParams& DP, const std::vector<DevDomain>& doms, long long ntot, cudaStream_t st,
                           int* err);

@@ -1,0 +1,983 @@
+// The per-direction kernels of the per-timestep update (reconstruction, face
+// flux, update), one source for two working types: PT = DevParams (binary64,
+// the reference's evaluation order: bit-exact parity, compiled with
+// -fmad=false in tj_fp64.cu) and PT = DevParams32 (binary32 bulk, tj_fp32.cu).
+// The binary32 instance keeps the total energy as a compensated pair (E, Elo),
+// closes the pressure in binary64 (in c2p) and projects onto the yield
+// surface in binary64 (plastic_cell_in64); everything else is the same code.
+//
+// One RK stage (HLLCadvance, hllc.cpp:579-695) is, per direction d:
+//   k_recon   per cell : MUSCL (hllc.cpp:541-575), BVD-THINC (thinc.cpp:67-208),
+//                        cleanUpAlpha of the reconstructed states (hllc.cpp:628-629),
+//                        primitiveToConservative + getSoundSpeed (634-638)
+//   k_flux    per face : HLLC (hllc.cpp:384-487) or 5-wave (133-380)
+//   k_update  per cell : update (hllc.cpp:493-523); after the last direction
+//                        conservativeToPrimitive (689), and at the end of the
+//                        second stage the RK2 average (705), plasticUpdate,
+//                        cleanUpV, cleanUpAlpha and the NaN check
+//                        (main.cpp:145-187).
+// Ghost cells are never stored: a read outside a domain maps the index back
+// (foextrap: nearest cell; reflect: mirror, negating the normal velocity and
+// momentum), which is what the reference's FillDomainBoundary and
+// FillBoundary calls leave in the ghost cells (main.cpp:124-126,
+// hllc.cpp:642-646,690-691).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "tj_device.cuh"
+#include "tj_fp64.cuh"
+
+namespace tj {
+
+// Error-free accumulation of b into the pair (hi, lo) (binary32 energy).
+__device__ __forceinline__ void dd_add32(float& hi, float& lo, float b)
+{
+    const float s = __fadd_rn(hi, b);
+    const float bb = __fsub_rn(s, hi);
+    const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    lo = __fadd_rn(lo, e);
+    const float t = __fadd_rn(s, lo);
+    lo = __fsub_rn(lo, __fsub_rn(t, s));
+    hi = t;
+}
+
+// (ah + al) / 2 + (bh + bl) / 2 into (bh, bl) (the RK2 average of the energy).
+__device__ __forceinline__ void avg_pair32(float ah, float al, float& bh, float& bl)
+{
+    float hs = 0.5f * ah, ls = 0.5f * al;
+    dd_add32(hs, ls, 0.5f * bh);
+    ls = __fadd_rn(ls, 0.5f * bl);
+    const float t = __fadd_rn(hs, ls);
+    bl = __fsub_rn(ls, __fsub_rn(t, hs));
+    bh = t;
+}
+
+__device__ __forceinline__ int find_dom(const DevDomain* doms, int ndom, long long g)
+{
+    int lo = 0, hi = ndom - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (doms[mid].off <= g) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ int find_dom_face(const DevDomain* doms, int ndom, int d, long long f)
+{
+    int lo = 0, hi = ndom - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (doms[mid].foff[d] <= f) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ void set_status(DevScalars* s, int code)
+{
+    atomicCAS(&s->status, 0, code);
+}
+
+// Map (i,j,k), possibly outside the domain, to a valid cell; refl[d] = 1 when
+// direction d reflected.
+template <typename PT, typename R = typename PT::real>
+__device__ __forceinline__ long long map_cell(const PT& P, const DevDomain& D, int i, int j, int k, int* refl)
+{
+    int ijk[3] = {i, j, k};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        refl[d] = 0;
+        if (d >= P.dim) continue;
+        int n = D.n[d];
+        if (ijk[d] < 0) {
+            if (P.lo_bc[d] == TJ_BC_REFLECTIVE) { ijk[d] = -1 - ijk[d]; refl[d] = 1; }
+            else ijk[d] = 0;
+        } else if (ijk[d] > n - 1) {
+            if (P.hi_bc[d] == TJ_BC_REFLECTIVE) { ijk[d] = 2 * n - 1 - ijk[d]; refl[d] = 1; }
+            else ijk[d] = n - 1;
+        }
+    }
+    return D.off + ijk[0] + (long long)D.n[0] * (ijk[1] + (long long)D.n[1] * ijk[2]);
+}
+
+__device__ __forceinline__ long long face_index(const DevDomain& D, int d, int i, int j, int k)
+{
+    int nf0 = D.n[0] + (d == 0), nf1 = D.n[1] + (d == 1);
+    return D.foff[d] + i + (long long)nf0 * (j + (long long)nf1 * k);
+}
+
+// Carried-state load with the reflect_odd sign applied.
+template <typename PT, typename R = typename PT::real>
+__device__ inline void load_state(const PT& P, const R* X, long long nt, long long g, const int* refl,
+                                  CellT<R>& c)
+{
+    for (int m = 0; m < P.M; ++m) {
+        c.alpha[m] = X[(P.S_ALPHA + m) * nt + g];
+        c.arho[m] = X[(P.S_ARHO + m) * nt + g];
+        c.rhok[m] = X[(P.S_RHOK + m) * nt + g];
+    }
+    c.rho = X[P.S_RHO * nt + g];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        R u = X[(P.S_VEL + r) * nt + g], ru = X[(P.S_RHOU + r) * nt + g];
+        if (refl && refl[r]) { u = -u; ru = -ru; }
+        c.vel[r] = u;
+        c.rhou[r] = ru;
+    }
+    c.E = X[P.S_E * nt + g];
+    if constexpr (sizeof(R) == 4) c.Elo = X[P.S_ELO * nt + g];
+    c.p = X[P.S_P * nt + g];
+    c.hj2 = R(0.0);
+    if (P.solid) {
+#pragma unroll
+        for (int q = 0; q < 9; ++q) c.V[q] = X[(P.S_V + q) * nt + g];
+        c.hj2 = X[P.S_HJ2 * nt + g];
+    }
+    if (P.plastic)
+        for (int m = 0; m < P.M; ++m) {
+            c.eps[m] = X[(P.S_EPS + m) * nt + g];
+            c.are[m] = X[(P.S_ARE + m) * nt + g];
+        }
+}
+
+template <typename PT, typename R = typename PT::real>
+__device__ inline void store_state(const PT& P, R* X, long long nt, long long g, const CellT<R>& c)
+{
+    for (int m = 0; m < P.M; ++m) {
+        X[(P.S_ALPHA + m) * nt + g] = c.alpha[m];
+        X[(P.S_ARHO + m) * nt + g] = c.arho[m];
+        X[(P.S_RHOK + m) * nt + g] = c.rhok[m];
+    }
+    X[P.S_RHO * nt + g] = c.rho;
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        X[(P.S_VEL + r) * nt + g] = c.vel[r];
+        X[(P.S_RHOU + r) * nt + g] = c.rhou[r];
+    }
+    X[P.S_E * nt + g] = c.E;
+    if constexpr (sizeof(R) == 4) X[P.S_ELO * nt + g] = c.Elo;
+    X[P.S_P * nt + g] = c.p;
+    if (P.solid) {
+#pragma unroll
+        for (int q = 0; q < 9; ++q) X[(P.S_V + q) * nt + g] = c.V[q];
+        X[P.S_HJ2 * nt + g] = c.hj2;
+    }
+    if (P.plastic)
+        for (int m = 0; m < P.M; ++m) {
+            X[(P.S_EPS + m) * nt + g] = c.eps[m];
+            X[(P.S_ARE + m) * nt + g] = c.are[m];
+        }
+}
+
+template <typename PT, typename R = typename PT::real>
+__device__ inline void store_face(const PT& P, R* F, long long nt, long long g, const CellT<R>& c)
+{
+    for (int m = 0; m < P.M; ++m) {
+        F[(P.F_ALPHA + m) * nt + g] = c.alpha[m];
+        F[(P.F_ARHO + m) * nt + g] = c.arho[m];
+    }
+    F[P.F_RHO * nt + g] = c.rho;
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        F[(P.F_RHOU + r) * nt + g] = c.rhou[r];
+        F[(P.F_VEL + r) * nt + g] = c.vel[r];
+    }
+    F[P.F_E * nt + g] = c.E;
+    F[P.F_P * nt + g] = c.p;
+    F[P.F_A * nt + g] = c.a;
+    if (P.solid) {
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+            F[(P.F_SIGMA + q) * nt + g] = c.sigma[q];
+            F[(P.F_V + q) * nt + g] = c.V[q];
+        }
+    }
+    if (P.plastic)
+        for (int m = 0; m < P.M; ++m) F[(P.F_ARE + m) * nt + g] = c.are[m];
+}
+
+template <typename PT, typename R = typename PT::real>
+__device__ inline void load_face(const PT& P, const R* F, long long nt, long long g, int oddir, CellT<R>& c)
+{
+    for (int m = 0; m < P.M; ++m) {
+        c.alpha[m] = F[(P.F_ALPHA + m) * nt + g];
+        c.arho[m] = F[(P.F_ARHO + m) * nt + g];
+        c.rhok[m] = R(0.0);
+    }
+    c.rho = F[P.F_RHO * nt + g];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        R u = F[(P.F_VEL + r) * nt + g], ru = F[(P.F_RHOU + r) * nt + g];
+        if (r == oddir) { u = -u; ru = -ru; }
+        c.vel[r] = u;
+        c.rhou[r] = ru;
+    }
+    c.E = F[P.F_E * nt + g];
+    c.p = F[P.F_P * nt + g];
+    c.a = F[P.F_A * nt + g];
+    c.hj2 = R(0.0);
+    if (P.solid) {
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+            c.sigma[q] = F[(P.F_SIGMA + q) * nt + g];
+            c.V[q] = F[(P.F_V + q) * nt + g];
+        }
+    } else {
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+            for (int q = 0; q < 3; ++q) c.sigma[3 * r + q] = -c.p * (R)(r == q);  // stressTensor, fluid
+    }
+    if (P.plastic)
+        for (int m = 0; m < P.M; ++m) c.are[m] = F[(P.F_ARE + m) * nt + g];
+}
+
+template <typename R>
+__device__ __forceinline__ R vanleer(R r)  // hllc.cpp:527-537
+{
+    if (r <= R(0.0)) return R(0.0);
+    R a = R(2.0) / (R(1.0) + r), b = R(2.0) * r / (R(1.0) + r);
+    return (b < a) ? b : a;
+}
+
+template <typename R>
+__device__ __forceinline__ void muscl1(R um, R u0, R up, R& l, R& r)  // hllc.cpp:557-568
+{
+    R rr = (u0 - um) / (up - u0);
+    if (isinf(rr) || isnan(rr)) rr = R(0.0);
+    R grad = vanleer(rr) * R(0.5) * (up - um);
+    l = u0 - R(0.5) * grad;
+    r = u0 + R(0.5) * grad;
+}
+
+// One carried word at a possibly-ghost cell.
+template <typename PT, typename R = typename PT::real>
+__device__ __forceinline__ R gv(const PT& P, const DevDomain& D, const R* X, long long nt, int word,
+                                     int i, int j, int k)
+{
+    int refl[3];
+    long long g = map_cell(P, D, i, j, k, refl);
+    R v = X[word * nt + g];
+    for (int d = 0; d < P.dim; ++d)
+        if (refl[d] && (word == P.S_VEL + d || word == P.S_RHOU + d)) v = -v;
+    return v;
+}
+
+// ---------------------------------------------------------------------------
+// BVD-THINC candidate of one cell (thinc.cpp:67-147).
+// ---------------------------------------------------------------------------
+template <typename R>
+struct ThincCand {
+    int mixed[TJ_MAX_MAT];
+    R L[TJ_MAX_MAT], Rv[TJ_MAX_MAT];
+    int flag;
+};
+
+template <typename PT, typename R = typename PT::real>
+__device__ inline R youngs(const PT& P, const DevDomain& D, const R* X, long long nt, int m, int i,
+                                int j, int k, int d)  // thinc.cpp:28-53
+{
+    int a = P.S_ALPHA + m;
+#define NB(di, dj) gv(P, D, X, nt, a, i + (di), j + (dj), k)
+    R nx = -R(1.0) / (R(8.0) * (R)D.dx[0]) * (NB(1, 1) + R(2.0) * NB(1, 0) + NB(1, -1) - NB(-1, 1) - R(2.0) * NB(-1, 0) - NB(-1, -1));
+    R ny = -R(1.0) / (R(8.0) * (R)D.dx[1]) * (NB(1, 1) + R(2.0) * NB(0, 1) + NB(-1, 1) - NB(-1, -1) - R(2.0) * NB(0, -1) - NB(1, -1));
+#undef NB
+    R norm = sqrt(nx * nx + ny * ny);
+    if (norm < R(1E-20)) return 0;
+    return d == 0 ? fabs(nx / norm) : fabs(ny / norm);
+}
+
+template <typename PT, typename R = typename PT::real>
+__device__ inline void thinc_cand(const PT& P, const DevDomain& D, const R* X, long long nt, int i, int j,
+                                  int k, int d, ThincCand<R>& t)
+{
+    const R eps = R(1E-20), beta0 = P.beta;
+    int o[3] = {0, 0, 0};
+    o[d] = 1;
+    t.flag = 0;
+    for (int m = 0; m < P.M; ++m) {
+        int a = P.S_ALPHA + m;
+        R aL = gv(P, D, X, nt, a, i - o[0], j - o[1], k - o[2]);
+        R aR = gv(P, D, X, nt, a, i + o[0], j + o[1], k + o[2]);
+        R a0 = gv(P, D, X, nt, a, i, j, k);
+        R mn = (aR < aL) ? aR : aL;
+        R mx = ((aL < aR) ? aR : aL) - mn;
+        R theta = (R)((R(0.0) < aR - aL) - (aR - aL < R(0.0)));
+        R C = (mx < eps) ? R(0.0) : (a0 - mn + eps) / (mx + eps);
+        R delta = R(1E-4);
+        int mixed = (C > delta) && (C < (R(0.999999) - delta)) && ((aR - a0) * (a0 - aL) >= R(0.0));
+        t.mixed[m] = mixed;
+        t.flag = mixed;  // the last material wins (thinc.cpp:110-114)
+        t.L[m] = R(0.0);
+        t.Rv[m] = R(0.0);
+        if (mixed) {
+            R nvc = (P.dim == 2) ? youngs(P, D, X, nt, m, i, j, k, d) : R(1.0);
+            R beta = nvc * beta0 + R(0.01);
+            R coshB = tjm_cosh(beta), tanhB = tjm_tanh(beta);
+            R B = tjm_exp(theta * beta * ((R(2.0) * C) - R(1.0)));
+            R A = ((B / coshB) - R(1.0)) / tanhB;
+            t.Rv[m] = mn + (mx / R(2.0)) * (R(1.0) + theta * ((tanhB + A) / (R(1.0) + A * tanhB)));
+            t.L[m] = mn + (mx / R(2.0)) * (R(1.0) + theta * A);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Reconstruction of one direction.
+// ---------------------------------------------------------------------------
+template <typename PT, typename R = typename PT::real>
+__global__ void k_recon(PT P, PathBufs<typename PT::real> b, const R* __restrict__ X, int d)
+{
+    if (b.scal->done) return;
+    const long long nt = b.ntot;
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < nt; g += (long long)gridDim.x * blockDim.x) {
+        const int q = find_dom(b.doms, b.ndom, g);
+        const DevDomain D = b.doms[q];
+        long long l = g - D.off;
+        int i = (int)(l % D.n[0]), j = (int)((l / D.n[0]) % D.n[1]), k = (int)(l / ((long long)D.n[0] * D.n[1]));
+        int o[3] = {0, 0, 0};
+        o[d] = 1;
+        int rm[3], rp[3];
+        long long gm = map_cell(P, D, i - o[0], j - o[1], k - o[2], rm);
+        long long gp = map_cell(P, D, i + o[0], j + o[1], k + o[2], rp);
+        CellT<R> um, u0, up, L, Rc;
+        load_state(P, X, nt, gm, rm, um);
+        load_state(P, X, nt, g, nullptr, u0);
+        load_state(P, X, nt, gp, rp, up);
+        L = u0;
+        Rc = u0;
+        if (P.muscl) {  // MUSCLextrapolate over the primitive list
+            for (int m = 0; m < P.M; ++m) {
+                muscl1(um.alpha[m], u0.alpha[m], up.alpha[m], L.alpha[m], Rc.alpha[m]);
+                muscl1(um.rhok[m], u0.rhok[m], up.rhok[m], L.rhok[m], Rc.rhok[m]);
+            }
+#pragma unroll
+            for (int r = 0; r < 3; ++r) muscl1(um.vel[r], u0.vel[r], up.vel[r], L.vel[r], Rc.vel[r]);
+            muscl1(um.p, u0.p, up.p, L.p, Rc.p);
+            if (P.solid)
+#pragma unroll
+                for (int qq = 0; qq < 9; ++qq) muscl1(um.V[qq], u0.V[qq], up.V[qq], L.V[qq], Rc.V[qq]);
+            if (P.plastic)
+                for (int m = 0; m < P.M; ++m) muscl1(um.eps[m], u0.eps[m], up.eps[m], L.eps[m], Rc.eps[m]);
+        }
+        int reps = 0;
+        if (P.thinc) {
+            const int* bx = b.boxes + 6 * (D.box_off + b.cell_box[g]);
+            int idx[3] = {i, j, k};
+            const int in_m = idx[d] - 1 >= bx[d], in_p = idx[d] + 1 <= bx[3 + d];
+            reps = D.nbox - b.cell_box[g];
+            ThincCand<R> tc, tm, tp;
+            thinc_cand(P, D, X, nt, i, j, k, d, tc);
+            if (in_m) thinc_cand(P, D, X, nt, i - o[0], j - o[1], k - o[2], d, tm);
+            if (in_p) thinc_cand(P, D, X, nt, i + o[0], j + o[1], k + o[2], d, tp);
+            const long long gmm = D.off + (i - o[0]) + (long long)D.n[0] * ((j - o[1]) + (long long)D.n[1] * (k - o[2]));
+            const long long gpp = D.off + (i + o[0]) + (long long)D.n[0] * ((j + o[1]) + (long long)D.n[1] * (k + o[2]));
+            int code = 0;
+            for (int m = 0; m < P.M; ++m) {
+                const int a = P.S_ALPHA + m;
+                R urm, ulp, trm, tlp;
+                // UR.left / UL.right: MUSCL value inside the box, stage input in a ghost.
+                if (in_m) {
+                    R l_, r_;
+                    muscl1(gv(P, D, X, nt, a, i - 2 * o[0], j - 2 * o[1], k - 2 * o[2]), um.alpha[m], u0.alpha[m], l_, r_);
+                    urm = r_;
+                    trm = tm.mixed[m] ? tm.Rv[m] : b.urstar[(long long)m * nt + gmm];
+                } else {
+                    urm = um.alpha[m];
+                    trm = R(0.0);  // URStar ghosts are never written
+                }
+                if (in_p) {
+                    R l_, r_;
+                    muscl1(u0.alpha[m], up.alpha[m], gv(P, D, X, nt, a, i + 2 * o[0], j + 2 * o[1], k + 2 * o[2]), l_, r_);
+                    ulp = l_;
+                    tlp = tp.mixed[m] ? tp.L[m] : b.ulstar[(long long)m * nt + gpp];
+                } else {
+                    ulp = up.alpha[m];
+                    // ULStar's ghost at the box's hi+1 face: star alpha of the last flux pass along d
+                    tlp = b.gstar[d][(long long)m * b.nftot[d] + face_index(D, d, i + o[0], j + o[1], k + o[2])];
+                }
+                R tpl = tc.mixed[m] ? tc.L[m] : b.ulstar[(long long)m * nt + g];
+                R tpr = tc.mixed[m] ? tc.Rv[m] : b.urstar[(long long)m * nt + g];
+                R upl = L.alpha[m], upr = Rc.alpha[m];
+#define MN(x, y) (((y) < (x)) ? (y) : (x))
+#define TBV(PL, PR)                                                                                          \
+    MN(MN(fabs(urm - (PL)) + fabs((PR)-ulp), fabs(trm - (PL)) + fabs((PR)-tlp)),                            \
+       MN(fabs(urm - (PL)) + fabs((PR)-tlp), fabs(trm - (PL)) + fabs((PR)-ulp)))
+                R tbvm = TBV(upl, upr);
+                R tbvt = TBV(tpl, tpr);
+#undef TBV
+#undef MN
+                if (tc.flag && tbvt < tbvm) {
+                    L.alpha[m] = tpl;
+                    Rc.alpha[m] = tpr;
+                    code |= (tc.mixed[m] ? 1 : 2) << (2 * m);
+                }
+            }
+            if (b.rec) {
+                for (int m = 0; m < P.M; ++m) {
+                    b.rec[((long long)(d * 2) * P.M + m) * nt + g] = L.alpha[m];
+                    b.rec[((long long)(d * 2 + 1) * P.M + m) * nt + g] = Rc.alpha[m];
+                }
+                b.rec_code[(long long)d * nt + g] = code;
+            }
+            // THINC pass 1 writes its candidates into the persistent scratch.
+            for (int m = 0; m < P.M; ++m)
+                if (tc.mixed[m]) {
+                    b.ulstar[(long long)m * nt + g] = tc.L[m];
+                    b.urstar[(long long)m * nt + g] = tc.Rv[m];
+                }
+        }
+        // cleanUpAlpha of UL and UR: nbox-b times for box b, the closures see
+        // the first (hllc.cpp:628-638).
+        for (int side = 0; side < 2; ++side) {
+            CellT<R>& S = side ? Rc : L;
+            if (reps > 0) {
+                int e = cleanup_alpha(P, S.alpha);
+                if (e) set_status(b.scal, e);
+            }
+            p2c(P, S);
+            S.a = sound_speed(P, S);
+            for (int r = 1; r < reps; ++r) {
+                R before[TJ_MAX_MAT];
+                for (int m = 0; m < P.M; ++m) before[m] = S.alpha[m];
+                int e = cleanup_alpha(P, S.alpha);
+                if (e) set_status(b.scal, e);
+                bool same = true;
+                for (int m = 0; m < P.M; ++m)
+                    same &= (__double_as_longlong(before[m]) == __double_as_longlong(S.alpha[m]));
+                if (same) break;
+            }
+        }
+        store_face(P, b.UL, nt, g, L);
+        store_face(P, b.UR, nt, g, Rc);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Riemann solvers (hllc.cpp:1-487, flux.cpp:5-47).
+// ---------------------------------------------------------------------------
+template <typename PT, typename R = typename PT::real>
+__device__ inline void star_state(const PT& P, const CellT<R>& U, CellT<R>& Us, R SK, R Ss, int d)  // :12-73
+{
+    const R tol = R(1E-20);
+    R ud = U.vel[d];
+    R mult = (fabs((Ss - ud) / Ss) < tol ? R(1.0) : (SK - ud) / (SK - Ss));
+    Us.rho = R(0.0);
+    for (int m = 0; m < P.M; ++m) {
+        Us.alpha[m] = U.alpha[m];
+        Us.arho[m] = mult * U.arho[m];
+        Us.rhok[m] = Us.arho[m] / Us.alpha[m];
+        if (P.plastic && P.phase[m] == TJ_PHASE_SOLID) Us.are[m] = mult * U.are[m];
+        Us.rho += Us.arho[m];
+    }
+#pragma unroll
+    for (int row = 0; row < 3; ++row) {
+        if (row == d) Us.rhou[row] = mult * U.rho * Ss;
+        else Us.rhou[row] = mult * U.rhou[row];
+        Us.vel[row] = Us.rhou[row] / Us.rho;
+        if (P.solid)
+#pragma unroll
+            for (int col = 0; col < 3; ++col)
+                Us.V[3 * row + col] = (row == d) ? U.V[3 * row + col] : mult * U.V[3 * row + col];
+    }
+    Us.E = mult * U.rho * (U.E / U.rho + (Ss - ud) * (Ss - (U.sigma[4 * d]) / (U.rho * (SK - ud))));
+}
+
+// Physical flux of the conservative variables (flux.cpp:33-47) into the
+// flux-word layout.
+template <typename PT, typename R = typename PT::real>
+__device__ inline void phys_flux(const PT& P, const CellT<R>& U, int d, R* F)
+{
+    R ud = U.vel[d];
+    for (int m = 0; m < P.M; ++m) {
+        F[P.X_ALPHA + m] = U.alpha[m] * ud;
+        F[P.X_ARHO + m] = U.arho[m] * ud;
+    }
+#pragma unroll
+    for (int r = 0; r < 3; ++r) F[P.X_RHOU + r] = U.rhou[r] * ud - U.sigma[3 * r + d];
+    R vs = R(0.0);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) vs += U.vel[i] * U.sigma[3 * i + d];
+    F[P.X_E] = U.E * ud - vs;
+    if (P.solid)
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+            int row = q / 3, col = q % 3;
+            F[P.X_V + q] = U.V[q] * ud - U.V[3 * d + col] * U.vel[row];
+        }
+    if (P.plastic)
+        for (int m = 0; m < P.M; ++m) F[P.X_ARE + m] = U.are[m] * ud;
+}
+
+// Conservative values of a state in the flux-word layout.
+template <typename PT, typename R = typename PT::real>
+__device__ inline void cons_vals(const PT& P, const CellT<R>& U, R* Q)
+{
+    for (int m = 0; m < P.M; ++m) {
+        Q[P.X_ALPHA + m] = U.alpha[m];
+        Q[P.X_ARHO + m] = U.arho[m];
+    }
+#pragma unroll
+    for (int r = 0; r < 3; ++r) Q[P.X_RHOU + r] = U.rhou[r];
+    Q[P.X_E] = U.E;
+    if (P.solid)
+#pragma unroll
+        for (int q = 0; q < 9; ++q) Q[P.X_V + q] = U.V[q];
+    if (P.plastic)
+        for (int m = 0; m < P.M; ++m) Q[P.X_ARE + m] = U.are[m];
+}
+
+#define TJ_MAXX 32
+
+// Returns the side whose star alpha the face carries: 0 left, 1 right.
+template <typename PT, typename R = typename PT::real>
+__device__ inline int face_flux(const PT& P, const CellT<R>& L, const CellT<R>& Rc, int d, R* F, DevScalars* scal)
+{
+    R x1 = fabs(L.vel[d]) + L.a, x2 = fabs(Rc.vel[d]) + Rc.a;
+    R SR = (x1 < x2) ? x2 : x1;
+    R SL = -SR;
+    R Ss = (-Rc.sigma[4 * d] + L.sigma[4 * d] + L.rhou[d] * (SL - L.vel[d]) - Rc.rhou[d] * (SR - Rc.vel[d])) /
+                (L.rho * (SL - L.vel[d]) - Rc.rho * (SR - Rc.vel[d]));  // getSstar, hllc.cpp:5-8
+    F[P.X_SSTAR] = Ss;
+    const int nx = P.X_SSTAR;  // words before S*: the conservative variables
+    R FK[TJ_MAXX], QK[TJ_MAXX], QS[TJ_MAXX], FS[TJ_MAXX];
+    CellT<R> Ls, Rs;
+    if (!P.solid) {
+        int side;
+        const CellT<R>* K;
+        R SK;
+        bool hllc;
+        if (SL >= R(0.0)) { side = 0; K = &L; SK = SL; hllc = false; }
+        else if (Ss >= R(0.0)) { side = 0; K = &L; SK = SL; hllc = true; }
+        else if (SR >= R(0.0)) { side = 1; K = &Rc; SK = SR; hllc = true; }
+        else { side = 1; K = &Rc; SK = SR; hllc = false; }
+        CellT<R>& Ks = side ? Rs : Ls;
+        star_state(P, *K, Ks, SK, Ss, d);
+        phys_flux(P, *K, d, FK);
+        phys_flux(P, Ks, d, FS);
+        cons_vals(P, *K, QK);
+        cons_vals(P, Ks, QS);
+        for (int w = 0; w < nx; ++w) {
+            bool is_alpha = w < P.X_ALPHA + P.M;
+            F[w] = is_alpha ? FS[w] : (hllc ? FK[w] + SK * (QS[w] - QK[w]) : FK[w]);
+        }
+        return side;
+    }
+
+    // 5-wave solver for solids (hllc.cpp:133-380).
+    if (isnan(SL) || isnan(SR) || isnan(Ss)) { set_status(scal, TJ_ERR_WAVESPEED); return 0; }
+    R SLT = R(0.0), SRT = R(0.0);
+    CellT<R> Uss;
+    R QL[TJ_MAXX], QR[TJ_MAXX], QLs[TJ_MAXX], QRs[TJ_MAXX], QSS[TJ_MAXX], FL[TJ_MAXX], FR[TJ_MAXX], FAs[TJ_MAXX];
+    const R* vsrc;
+    int side;
+    auto starstar = [&](const CellT<R>& UK, CellT<R>& UKs, R SKT) {  // getStarStarState, hllc.cpp:87-129
+        Uss = UKs;
+#pragma unroll
+        for (int i = 0; i < 3; ++i)  // getSigmaStar, hllc.cpp:75-83
+            UKs.sigma[3 * i + d] =
+                (Ls.rho * (Ss - SLT) * Rs.rho * (Ss - SRT) * (L.vel[i] - Rc.vel[i]) + Ls.rho * (Ss - SLT) * Rc.sigma[3 * i + d] -
+                 Rs.rho * (Ss - SRT) * L.sigma[3 * i + d]) /
+                (Ls.rho * (Ss - SLT) - Rs.rho * (Ss - SRT));
+#pragma unroll
+        for (int row = 0; row < 3; ++row) {
+            if (row == d) continue;
+            Uss.rhou[row] += (UKs.sigma[3 * row + d] - UK.sigma[3 * row + d]) / (Ss - SKT);
+            Uss.vel[row] = Uss.rhou[row] / Uss.rho;
+        }
+#pragma unroll
+        for (int row = 0; row < 3; ++row) {
+            if (row == d) continue;
+            Uss.E += (Uss.vel[row] * UKs.sigma[3 * row + d] - UK.vel[row] * UK.sigma[3 * row + d]) / (Ss - SKT);
+#pragma unroll
+            for (int col = 0; col < 3; ++col)
+                Uss.V[3 * row + col] += (Uss.V[3 * d + col] * (Uss.vel[row] - UK.vel[row])) / (Ss - SKT);
+        }
+    };
+    phys_flux(P, L, d, FL);
+    phys_flux(P, Rc, d, FR);
+    cons_vals(P, L, QL);
+    cons_vals(P, Rc, QR);
+    if (SL >= R(0.0)) {
+        star_state(P, L, Ls, SL, Ss, d);
+        phys_flux(P, Ls, d, FAs);
+        for (int w = 0; w < nx; ++w) F[w] = (w < P.X_ALPHA + P.M) ? FAs[w] : FL[w];
+        vsrc = L.V;
+        side = 0;
+    } else if (Ss >= R(0.0)) {
+        star_state(P, L, Ls, SL, Ss, d);
+        SLT = Ss - transverse_speed(P, Ls);
+        phys_flux(P, Ls, d, FAs);
+        cons_vals(P, Ls, QLs);
+        if (SLT >= R(0.0)) {
+            for (int w = 0; w < nx; ++w) F[w] = (w < P.X_ALPHA + P.M) ? FAs[w] : FL[w] + SL * (QLs[w] - QL[w]);
+            vsrc = Ls.V;
+        } else {
+            star_state(P, Rc, Rs, SR, Ss, d);
+            SRT = Ss + transverse_speed(P, Rs);
+            starstar(L, Ls, SLT);
+            cons_vals(P, Uss, QSS);
+            for (int w = 0; w < nx; ++w)
+                F[w] = (w < P.X_ALPHA + P.M) ? FAs[w] : FL[w] + SL * (QLs[w] - QL[w]) + SLT * (QSS[w] - QLs[w]);
+            vsrc = Uss.V;
+        }
+        side = 0;
+    } else if (SR >= R(0.0)) {
+        star_state(P, Rc, Rs, SR, Ss, d);
+        SRT = Ss + transverse_speed(P, Rs);
+        phys_flux(P, Rs, d, FAs);
+        cons_vals(P, Rs, QRs);
+        if (SRT >= R(0.0)) {
+            star_state(P, L, Ls, SL, Ss, d);
+            SLT = Ss - transverse_speed(P, Ls);
+            starstar(Rc, Rs, SRT);
+            cons_vals(P, Uss, QSS);
+            for (int w = 0; w < nx; ++w)
+                F[w] = (w < P.X_ALPHA + P.M) ? FAs[w] : FR[w] + SR * (QRs[w] - QR[w]) + SRT * (QSS[w] - QRs[w]);
+            vsrc = Uss.V;
+        } else {
+            for (int w = 0; w < nx; ++w) F[w] = (w < P.X_ALPHA + P.M) ? FAs[w] : FR[w] + SR * (QRs[w] - QR[w]);
+            vsrc = Rs.V;
+        }
+        side = 1;
+    } else {
+        star_state(P, Rc, Rs, SR, Ss, d);
+        phys_flux(P, Rs, d, FAs);
+        for (int w = 0; w < nx; ++w) F[w] = (w < P.X_ALPHA + P.M) ? FAs[w] : FR[w];
+        vsrc = Rc.V;
+        side = 1;
+    }
+#pragma unroll
+    for (int col = 0; col < 3; ++col) F[P.X_VSTAR + col] = vsrc[3 * d + col];  // VSTAR(d, col), read by update
+    if (isnan(SL) || isnan(SR) || isnan(Ss) || isnan(SLT) || isnan(SRT)) set_status(scal, TJ_ERR_WAVESPEED);
+    return side;
+}
+
+template <typename PT, typename R = typename PT::real>
+__global__ void k_flux(PT P, PathBufs<typename PT::real> b, int d)
+{
+    if (b.scal->done) return;
+    const long long nt = b.ntot, nf = b.nftot[d];
+    for (long long f = blockIdx.x * (long long)blockDim.x + threadIdx.x; f < nf; f += (long long)gridDim.x * blockDim.x) {
+        const int q = find_dom_face(b.doms, b.ndom, d, f);
+        const DevDomain D = b.doms[q];
+        int nfv[3] = {D.n[0], D.n[1], D.n[2]};
+        nfv[d] += 1;
+        long long l = f - D.foff[d];
+        int i = (int)(l % nfv[0]), j = (int)((l / nfv[0]) % nfv[1]), k = (int)(l / ((long long)nfv[0] * nfv[1]));
+        int o[3] = {0, 0, 0};
+        o[d] = 1;
+        int rl[3], rr[3];
+        long long gl = map_cell(P, D, i - o[0], j - o[1], k - o[2], rl);
+        long long gr = map_cell(P, D, i, j, k, rr);
+        CellT<R> L, Rc;
+        load_face(P, b.UR, nt, gl, rl[d] ? d : -1, L);
+        load_face(P, b.UL, nt, gr, rr[d] ? d : -1, Rc);
+        R F[TJ_MAXX];
+        int side = face_flux(P, L, Rc, d, F, b.scal);
+        for (int w = 0; w < P.NX; ++w) b.FX[(long long)w * nf + f] = F[w];
+        if (P.thinc) {
+            const CellT<R>& src = side ? Rc : L;
+            int idx[3] = {i, j, k};
+            if (idx[d] < D.n[d]) {  // ULStar alpha at the valid cell of this face
+                long long g = D.off + i + (long long)D.n[0] * (j + (long long)D.n[1] * k);
+                for (int m = 0; m < P.M; ++m) b.ulstar[(long long)m * nt + g] = src.alpha[m];
+            }
+            if (idx[d] >= 1) {  // the ghost hi+1 of the box to the left, if this is its hi face
+                long long gL = D.off + (i - o[0]) + (long long)D.n[0] * ((j - o[1]) + (long long)D.n[1] * (k - o[2]));
+                const int* bx = b.boxes + 6 * (D.box_off + b.cell_box[gL]);
+                if (bx[3 + d] == idx[d] - 1)
+                    for (int m = 0; m < P.M; ++m) b.gstar[d][(long long)m * nf + f] = src.alpha[m];
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Plastic radial return (plastic.cpp:83-223) and cleanUpV (:476-528).
+// ---------------------------------------------------------------------------
+template <typename PT, typename R = typename PT::real>
+__device__ inline int plastic_cell(const PT& P, CellT<R>& c)
+{
+    R tsolid = R(0.0);
+    for (int m = 0; m < P.M; ++m)
+        if (P.phase[m] == TJ_PHASE_SOLID) tsolid += c.alpha[m];
+    if (tsolid <= R(0.5)) {  // cellIsMostlyFluid
+        for (int m = 0; m < P.M; ++m) { c.eps[m] = R(0.0); c.are[m] = R(0.0); }
+        return 0;
+    }
+    hencky(P, c);
+    R JT = R(0.0), JB = R(0.0), norm = R(0.0), J, Jn;
+    for (int m = 0; m < P.M; ++m) {
+        ECellT<R> e = ecell_of(c, m);
+        if (P.phase[m] == TJ_PHASE_SOLID) {
+            J = sqrt(c.hj2);
+            R G = eos_G(P, m, e);
+            if (G * J * sqrt(R(3.0)) > P.yield[m]) Jn = P.yield[m] / (sqrt(R(3.0)) * G);
+            else Jn = J;
+            c.eps[m] += sqrt(R(2.0) / R(3.0)) * (J - Jn);
+            c.are[m] = c.eps[m] * c.arho[m];
+        } else {
+            J = R(0.0);
+            Jn = R(0.0);
+            c.eps[m] = R(0.0);
+            c.are[m] = R(0.0);
+        }
+        JB += (eos_invG(P, m, e)) * J;
+        JT += (eos_invG(P, m, e)) * Jn;
+        norm += (eos_invG(P, m, e));
+    }
+    JB *= R(1.0) / norm;
+    JT *= R(1.0) / norm;
+    if (JB == R(0.0) && JT == R(0.0)) { JB = R(1.0); JT = R(1.0); }
+    R t1[9], t2[9], t2i[9];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            R& dv = c.devH[3 * r + q];
+            if (dv != R(0.0) && JB == R(0.0) && JT != R(0.0)) return TJ_ERR_PLASTIC;
+            dv *= JT / JB;
+            t1[3 * r + q] = (R)(r == q) + R(0.5) * dv;
+            t2[3 * r + q] = (R)(r == q) - R(0.5) * dv;
+        }
+    invert3(t2, t2i);
+    mm3(t2i, t1, c.V);
+    return 0;
+}
+
+template <typename PT, typename R = typename PT::real>
+__device__ inline void cleanup_v_cell(const PT& P, CellT<R>& c)
+{
+    R ta = R(0.0), ts = R(0.0);
+    for (int m = 0; m < P.M; ++m) {
+        ta += c.alpha[m];
+        if (P.phase[m] == TJ_PHASE_SOLID) ts += c.alpha[m];
+    }
+    R B[9], Sq[9];
+    mmT3(c.V, c.V, B);
+    sqrtm3(B, Sq);
+    R norm = tjm_pow(det3(Sq), -R(1.0) / R(3.0));
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int q = 0; q < 3; ++q) c.V[3 * r + q] = ((Sq[3 * r + q] * norm * ts) + (R)(r == q) * (ta - ts)) / ta;
+}
+
+// The radial return of a binary32 cell in binary64 (the yield projection),
+// followed by conservativeToPrimitive in binary64 (plastic.cpp:227-244).
+template <typename PT, typename R = typename PT::real>
+__device__ inline int plastic_cell_in64(const PT& P, CellT<R>& c)
+{
+    CellT<double> d;
+    for (int m = 0; m < TJ_MAX_MAT; ++m) {
+        d.alpha[m] = c.alpha[m];
+        d.arho[m] = c.arho[m];
+        d.rhok[m] = c.rhok[m];
+        d.eps[m] = c.eps[m];
+        d.are[m] = c.are[m];
+    }
+    d.rho = c.rho;
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        d.rhou[r] = c.rhou[r];
+        d.vel[r] = c.vel[r];
+    }
+    d.E = (double)c.E + (double)c.Elo;
+    d.Elo = 0.0;
+    d.p = c.p;
+    d.a = c.a;
+    d.hj2 = c.hj2;
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+        d.sigma[q] = c.sigma[q];
+        d.V[q] = c.V[q];
+        d.devH[q] = c.devH[q];
+    }
+    const int e = plastic_cell(P.d, d);
+    c2p(P.d, d);
+    for (int m = 0; m < TJ_MAX_MAT; ++m) {
+        c.alpha[m] = (R)d.alpha[m];
+        c.arho[m] = (R)d.arho[m];
+        c.rhok[m] = (R)d.rhok[m];
+        c.eps[m] = (R)d.eps[m];
+        c.are[m] = (R)d.are[m];
+    }
+    c.rho = (R)d.rho;
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        c.rhou[r] = (R)d.rhou[r];
+        c.vel[r] = (R)d.vel[r];
+    }
+    c.E = (R)d.E;
+    c.Elo = (R)(d.E - (double)c.E);
+    c.p = (R)d.p;
+    c.hj2 = (R)d.hj2;
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+        c.sigma[q] = (R)d.sigma[q];
+        c.V[q] = (R)d.V[q];
+        c.devH[q] = (R)d.devH[q];
+    }
+    return e;
+}
+
+// contains_nan over the conservative and primitive lists of one cell.
+template <typename PT, typename R = typename PT::real>
+__device__ inline bool cell_has_nan(const PT& P, const CellT<R>& c)
+{
+    bool n = false;
+    for (int m = 0; m < P.M; ++m) n |= isnan(c.alpha[m]) || isnan(c.arho[m]) || isnan(c.rhok[m]);
+#pragma unroll
+    for (int r = 0; r < 3; ++r) n |= isnan(c.rhou[r]) || isnan(c.vel[r]);
+    n |= isnan(c.E) || isnan(c.p);
+    if (P.solid)
+#pragma unroll
+        for (int q = 0; q < 9; ++q) n |= isnan(c.V[q]);
+    if (P.plastic)
+        for (int m = 0; m < P.M; ++m) n |= isnan(c.eps[m]) || isnan(c.are[m]);
+    return n;
+}
+
+// ---------------------------------------------------------------------------
+// Update of one direction; last direction: c2p; second stage: average and
+// the post-advance operators of main.cpp:145-187.
+// ---------------------------------------------------------------------------
+template <typename PT, typename R = typename PT::real>
+__global__ void k_update(PT P, PathBufs<typename PT::real> b, const R* __restrict__ X, R* Y, int d, int first, int last,
+                         int finish)
+{
+    if (b.scal->done) return;
+    const long long nt = b.ntot, nf = b.nftot[d];
+    const R dtdx_num = b.scal->dt;
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < nt; g += (long long)gridDim.x * blockDim.x) {
+        const int q = find_dom(b.doms, b.ndom, g);
+        const DevDomain D = b.doms[q];
+        long long l = g - D.off;
+        int i = (int)(l % D.n[0]), j = (int)((l / D.n[0]) % D.n[1]), k = (int)(l / ((long long)D.n[0] * D.n[1]));
+        int o[3] = {0, 0, 0};
+        o[d] = 1;
+        const long long f0 = face_index(D, d, i, j, k), f1 = face_index(D, d, i + o[0], j + o[1], k + o[2]);
+        CellT<R> U, Yc;
+        load_state(P, X, nt, g, nullptr, U);
+        if (first) Yc = U;
+        else load_state(P, Y, nt, g, nullptr, Yc);
+        const R dtdx = dtdx_num / (R)D.dx[d];
+#define FXW(w, f) b.FX[(long long)(w)*nf + (f)]
+        const R dS = FXW(P.X_SSTAR, f0) - FXW(P.X_SSTAR, f1);
+        for (int m = 0; m < P.M; ++m) {
+            Yc.alpha[m] += dtdx * (FXW(P.X_ALPHA + m, f0) - FXW(P.X_ALPHA + m, f1) - U.alpha[m] * (FXW(P.X_SSTAR, f0) - FXW(P.X_SSTAR, f1)));
+            Yc.arho[m] += dtdx * (FXW(P.X_ARHO + m, f0) - FXW(P.X_ARHO + m, f1));
+        }
+        (void)dS;
+#pragma unroll
+        for (int r = 0; r < 3; ++r) Yc.rhou[r] += dtdx * (FXW(P.X_RHOU + r, f0) - FXW(P.X_RHOU + r, f1));
+        if constexpr (sizeof(R) == 4) dd_add32(Yc.E, Yc.Elo, dtdx * (FXW(P.X_E, f0) - FXW(P.X_E, f1)));
+        else Yc.E += dtdx * (FXW(P.X_E, f0) - FXW(P.X_E, f1));
+        if (P.solid)
+#pragma unroll
+            for (int qq = 0; qq < 9; ++qq) {
+                int row = qq / 3, col = qq % 3;
+                Yc.V[qq] += dtdx * (FXW(P.X_V + qq, f0) - FXW(P.X_V + qq, f1) -
+                                    (R(2.0) / R(3.0)) * U.V[qq] * (FXW(P.X_SSTAR, f0) - FXW(P.X_SSTAR, f1)) +
+                                    U.vel[row] * (FXW(P.X_VSTAR + col, f0) - FXW(P.X_VSTAR + col, f1)));
+            }
+        if (P.plastic)
+            for (int m = 0; m < P.M; ++m) Yc.are[m] += dtdx * (FXW(P.X_ARE + m, f0) - FXW(P.X_ARE + m, f1));
+#undef FXW
+        if (last) {
+            c2p(P, Yc);
+            if (finish) {
+                // U1 = U*0.5 + U2*0.5 over every carried component (hllc.cpp:705)
+                CellT<R> A0;
+                load_state(P, b.A, nt, g, nullptr, A0);
+                for (int m = 0; m < P.M; ++m) {
+                    Yc.alpha[m] = (A0.alpha[m] * (R(1.0) / R(2.0))) + (Yc.alpha[m] * (R(1.0) / R(2.0)));
+                    Yc.arho[m] = (A0.arho[m] * (R(1.0) / R(2.0))) + (Yc.arho[m] * (R(1.0) / R(2.0)));
+                    Yc.rhok[m] = (A0.rhok[m] * (R(1.0) / R(2.0))) + (Yc.rhok[m] * (R(1.0) / R(2.0)));
+                    if (P.plastic) {
+                        Yc.eps[m] = (A0.eps[m] * (R(1.0) / R(2.0))) + (Yc.eps[m] * (R(1.0) / R(2.0)));
+                        Yc.are[m] = (A0.are[m] * (R(1.0) / R(2.0))) + (Yc.are[m] * (R(1.0) / R(2.0)));
+                    }
+                }
+                Yc.rho = (A0.rho * (R(1.0) / R(2.0))) + (Yc.rho * (R(1.0) / R(2.0)));
+#pragma unroll
+                for (int r = 0; r < 3; ++r) {
+                    Yc.rhou[r] = (A0.rhou[r] * (R(1.0) / R(2.0))) + (Yc.rhou[r] * (R(1.0) / R(2.0)));
+                    Yc.vel[r] = (A0.vel[r] * (R(1.0) / R(2.0))) + (Yc.vel[r] * (R(1.0) / R(2.0)));
+                }
+                if constexpr (sizeof(R) == 4) avg_pair32(A0.E, A0.Elo, Yc.E, Yc.Elo);
+                else Yc.E = (A0.E * (R(1.0) / R(2.0))) + (Yc.E * (R(1.0) / R(2.0)));
+                Yc.p = (A0.p * (R(1.0) / R(2.0))) + (Yc.p * (R(1.0) / R(2.0)));
+                if (P.solid) {
+#pragma unroll
+                    for (int qq = 0; qq < 9; ++qq) Yc.V[qq] = (A0.V[qq] * (R(1.0) / R(2.0))) + (Yc.V[qq] * (R(1.0) / R(2.0)));
+                    Yc.hj2 = (A0.hj2 * (R(1.0) / R(2.0))) + (Yc.hj2 * (R(1.0) / R(2.0)));
+                }
+                if (finish == 2) {  // advance() alone: the average only
+                    store_state(P, b.A, nt, g, Yc);
+                    continue;
+                }
+                if (P.plastic) {
+                    int e;
+                    if constexpr (sizeof(R) == 4) e = plastic_cell_in64(P, Yc);
+                    else {
+                        e = plastic_cell(P, Yc);
+                        c2p(P, Yc);
+                    }
+                    if (e) set_status(b.scal, e);
+                }
+                if (P.solid) cleanup_v_cell(P, Yc);
+                int e = cleanup_alpha(P, Yc.alpha);
+                if (e) set_status(b.scal, e);
+                if (b.cell_box[g] == D.nbox - 1 && cell_has_nan(P, Yc)) atomicOr(&b.scal->nan_flag, 1);
+                store_state(P, b.A, nt, g, Yc);
+                continue;
+            }
+        }
+        store_state(P, Y, nt, g, Yc);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// CFL (timestep.cpp:7-70) and device-side time bookkeeping (main.cpp:121-143).
+// ---------------------------------------------------------------------------
+template <typename PT, typename R = typename PT::real>
+__global__ void k_cfl(PT P, PathBufs<typename PT::real> b, const R* __restrict__ X)
+{
+    if (b.scal->done) return;
+    const long long nt = b.ntot;
+    R mn = R(sizeof(R) == 4 ? 3.0e38 : 1.79769313486231570815e+308);
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < nt; g += (long long)gridDim.x * blockDim.x) {
+        const int q = find_dom(b.doms, b.ndom, g);
+        const DevDomain D = b.doms[q];
+        CellT<R> c;
+        load_state(P, X, nt, g, nullptr, c);
+        R a = sound_speed(P, c);
+        for (int n = 0; n < P.dim; ++n) {
+            R v = (R)D.dx[n] / (a + fabs(c.vel[n]));
+            if (v < mn) mn = v;
+        }
+    }
+    for (int s = 16; s > 0; s >>= 1) {
+        R o = __shfl_down_sync(0xffffffffu, mn, s);
+        if (o < mn) mn = o;
+    }
+    __shared__ R red[32];
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) red[w] = mn;
+    __syncthreads();
+    if (w == 0) {
+        mn = (lane < (int)(blockDim.x >> 5)) ? red[lane] : R(sizeof(R) == 4 ? 3.0e38 : 1.79769313486231570815e+308);
+        for (int s = 16; s > 0; s >>= 1) {
+            R o = __shfl_down_sync(0xffffffffu, mn, s);
+            if (o < mn) mn = o;
+        }
+        if (lane == 0) atomicMin(&b.scal->dtmin_bits, (unsigned long long)__double_as_longlong((double)mn));
+    }
+
+}
+
+}  // namespace tj

@@ -10,6 +10,7 @@ namespace tj {
 // Device copy of the solver parameters plus the layouts of the device
 // arrays (component offsets). Passed to kernels by value.
 struct DevParams {
+    using real = double;
     int dim, M, solid, thinc, plastic, muscl, any_solid;
     int fused64;  // fused kernels in binary64 (TJ_PRECISION_FUSED64)
     int lo_bc[3], hi_bc[3];
@@ -26,6 +27,26 @@ struct DevParams {
     // AccessPattern (reference component order)
     int A_ALPHA, A_ARHO, A_RHOK, A_RHO, A_RHOU, A_VEL, A_E, A_P, A_A, A_USTAR, A_SIGMA, A_V, A_VSTAR, A_DEVH, A_HJ2,
         A_EPS, A_ARE, NCOMP;
+    int S_ELO;  // binary32 state only (the low word of the energy); -1 here
+};
+
+// The same block for the binary32 instance of the per-direction kernels: the
+// EOS parameters in binary32, the carried state one word longer (S_ELO), and
+// the binary64 block for the pressure closure and the yield projection.
+struct DevParams32 {
+    using real = float;
+    int dim, M, solid, thinc, plastic, muscl, any_solid;
+    int fused64;
+    int lo_bc[3], hi_bc[3];
+    float cfl, beta;
+    int phase[TJ_MAX_MAT], eos[TJ_MAX_MAT];
+    float prm[TJ_MAX_MAT][TJ_MAX_EOS_PARAMS];
+    float yield[TJ_MAX_MAT];
+    int S_ALPHA, S_ARHO, S_RHOK, S_RHO, S_RHOU, S_VEL, S_E, S_P, S_V, S_HJ2, S_EPS, S_ARE, NS;
+    int F_ALPHA, F_ARHO, F_RHO, F_RHOU, F_VEL, F_E, F_P, F_A, F_SIGMA, F_V, F_ARE, NF;
+    int X_ALPHA, X_ARHO, X_RHOU, X_E, X_SSTAR, X_V, X_VSTAR, X_ARE, NX;
+    int S_ELO;
+    DevParams d;
 };
 
 // One independent domain: valid cells [0,n) per axis, stored contiguously

@@ -1,0 +1,59 @@
+"""Plotfile and gnuplot output in the reference's formats (host side)."""
+import os
+
+import numpy as np
+
+from tenjin_gb300 import cases, output
+
+
+def _state(case, seed=0):
+    d = case.domains[0]
+    n = len(output.variable_names(case))
+    return np.random.default_rng(seed).standard_normal((n, d.n_cells[2], d.n_cells[1], d.n_cells[0]))
+
+
+def test_variable_names_follow_the_access_pattern():
+    fl = output.variable_names(cases.shock_bubble_2d(n=8))
+    assert fl[:4] == ["alpha0_00", "alpha1_00", "alphaRho0_00", "alphaRho1_00"]
+    assert fl[6] == "rho0_00" and fl[7:10] == ["rhoU0_00", "rhoU0_10", "rhoU0_20"]
+    assert fl[-9:] == [f"sigma0_{r}{c}" for r in range(3) for c in range(3)]
+    assert len(fl) == 26  # two fluids: the reference's Ncomp
+    so = output.variable_names(cases.copper_plate_3d(n=4))
+    assert len(so) == 53 and so[-2:] == ["epsilon0_00", "alphaRhoEpsilon0_00"]
+    assert "HenckyJ20_00" in so
+
+
+def test_plotfile_round_trip_2d(tmp_path):
+    c = cases.shock_bubble_2d(n=24, max_grid_size=10)
+    st = _state(c)
+    p = output.write_plotfile(str(tmp_path / output.plotfile_name("plt", 7)), c, st, 1.25e-4, 7)
+    assert p.endswith("plt00007")
+    r = output.read_plotfile(p)
+    assert r["names"] == output.variable_names(c)
+    assert r["time"] == 1.25e-4 and r["dim"] == 2
+    assert np.array_equal(r["state"], st)
+    head = open(os.path.join(p, "Header")).read().split("\n")
+    assert head[0] == "HyperCLaw-V1.1" and head[-2] == "Level_0/Cell"
+    cell_h = open(os.path.join(p, "Level_0", "Cell_H")).read()
+    assert cell_h.count("FabOnDisk: Cell_D_00000") == len(c.domains[0].boxes)
+
+
+def test_plotfile_round_trip_3d_solid(tmp_path):
+    c = cases.copper_plate_3d(n=10, max_grid_size=6)
+    st = _state(c, 1)
+    r = output.read_plotfile(output.write_plotfile(str(tmp_path / "plt00000"), c, st, 0.0, 0))
+    assert np.array_equal(r["state"], st)
+
+
+def test_gnuplot_dump(tmp_path):
+    c = cases.sod_1d(ncells=40, max_grid_size=16)
+    st = _state(c)
+    files = output.write_gnuplot(str(tmp_path), c, st, 3)
+    assert [os.path.basename(f) for f in files] == ["rho03", "p03", "u03", "E03", "rhoU03", "alpha003"]
+    lines = open(files[0]).read().splitlines()
+    # box-list (MFIter) order, one line per cell
+    first = c.domains[0].boxes[0][0]
+    assert len(lines) == 40 and int(lines[0].split()[0]) == first
+    vals = {int(l.split()[0]): float(l.split()[1]) for l in lines}
+    assert sorted(vals) == list(range(40))
+    assert vals[5] == float(f"{st[3 * c.M, 0, 0, 5]:g}")
