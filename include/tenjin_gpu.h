@@ -75,7 +75,8 @@ typedef struct tj_params {
     int dim;          /* AMREX_SPACEDIM: 1, 2 or 3 */
     int n_materials;  /* numberOfMaterials */
     int n_mixtures;   /* numberOfMixtures: must be 0 */
-    int SOLID, THINC, RADIAL, PLASTIC, REACTIVE, MUSCL; /* RADIAL, REACTIVE: must be 0 */
+    int SOLID, THINC, RADIAL, PLASTIC, REACTIVE, MUSCL; /* REACTIVE: must be 0; RADIAL: not with
+                                                          elastic solids (SOLID without PLASTIC) */
     int nghost;       /* Nghost: must be >= 2 */
     int lo_bc[3], hi_bc[3];
     double CFL, THINCbeta;
@@ -131,6 +132,12 @@ int tj_compute_dt(tj_ctx* ctx, double* dt);
 int tj_advance(tj_ctx* ctx, double dt);
 /* PlasticEOS::plasticUpdate (plastic.cpp:227-244), radial return. */
 int tj_plastic_update(tj_ctx* ctx, double dt);
+/* geometricSourceTerm (radial.cpp:37-54): the radial source of a spherical
+ * (1-D) or cylindrical (2-D, 3-D) problem with x the radius, then
+ * conservativeToPrimitive. The stress it reads is the state's as its last
+ * conservativeToPrimitive left it. tj_step applies it after plasticUpdate
+ * when RADIAL is set (main.cpp:159-161). */
+int tj_geometric_source(tj_ctx* ctx, double dt);
 /* CellArray::cleanUpV (boxaccesscellarray.cpp:476-528). */
 int tj_cleanup_v(tj_ctx* ctx);
 /* CellArray::cleanUpAlpha (boxaccesscellarray.cpp:530-599). */
@@ -144,7 +151,8 @@ int tj_contains_nan(tj_ctx* ctx, int* flag);
 
 /* One iteration of the time loop of main.cpp:121-191 with dt and t kept on
  * the device: dt = getTimeStep, clamped to t_end, times 0.2 for the first
- * five steps; advance; plasticUpdate (PLASTIC); cleanUpV (SOLID);
+ * five steps; advance; plasticUpdate (PLASTIC); geometricSourceTerm (RADIAL);
+ * cleanUpV (SOLID);
  * cleanUpAlpha; NaN check. Does not synchronise. */
 int tj_step(tj_ctx* ctx, double t_end);
 /* Run up to nsteps iterations or until t >= t_end. Steps are issued in

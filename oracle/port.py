@@ -30,6 +30,7 @@ class _Params(ctypes.Structure):
         ("phase", ctypes.c_int * MAX_MAT), ("eos", ctypes.c_int * MAX_MAT),
         ("eos_params", (ctypes.c_double * MAX_PARAMS) * MAX_MAT),
         ("yield_stress", ctypes.c_double * MAX_MAT),
+        ("radial", ctypes.c_int),
     ]
 
 
@@ -86,6 +87,7 @@ def make_params(case) -> _Params:
     for d in range(3):
         p.lo_bc[d], p.hi_bc[d] = case.lo_bc[d], case.hi_bc[d]
     p.cfl, p.thinc_beta = case.cfl, case.thinc_beta
+    p.radial = getattr(case, "radial", 0)
     for m, mat in enumerate(case.materials):
         p.phase[m], p.eos[m] = mat.phase, mat.eos
         for q, v in enumerate(mat.params):

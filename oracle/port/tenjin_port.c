@@ -1281,6 +1281,41 @@ static double domain_dt(tjp_sim* s, pdom* D)
     return s->p.cfl * dtmin;
 }
 
+/* addGeometricSourceTerm (radial.cpp:5-31) on one cell: every conservative
+ * variable gains dt * (multiplier / r) * geometricFlux (flux.cpp:51-77), with
+ * r = (i + 0.5) dx[0] and multiplier -2 in 1-D (spherical), -1 otherwise
+ * (cylindrical). The fluxes read the velocity and the stress the state holds,
+ * which the loop over the conservative variables does not change. */
+static void radial_cell(tjp_sim* s, const pdom* D, double* X, long N, long c, double dt)
+{
+    const cmap* C = &s->c;
+    const int M = s->p.M;
+    const int i = (int)(c % D->n[0]);
+    const double mult = (s->p.dim == 1 ? -2.0 : -1.0);
+    const double inv_r = mult / (((double)i + 0.5) * D->dx[0]);
+    const double u = AT(X, C->VEL, c);
+#define SG(r, q) AT(X, C->SIGMA + 3 * (r) + (q), c)
+    for (int m = 0; m < M; ++m) AT(X, C->ALPHA + m, c) += dt * inv_r * 0.0;
+    for (int m = 0; m < M; ++m) AT(X, C->ALPHARHO + m, c) += dt * inv_r * (AT(X, C->ALPHARHO + m, c) * u);
+    AT(X, C->RHOU + 0, c) += dt * inv_r * (AT(X, C->RHOU + 0, c) * u - SG(0, 0) + SG(2, 2));
+    AT(X, C->RHOU + 1, c) += dt * inv_r * (AT(X, C->RHOU + 1, c) * u - SG(0, 1));
+    AT(X, C->RHOU + 2, c) += dt * inv_r * (-2.0 * SG(0, 2));
+    double vds = 0.0; /* vdotsigma (flux.cpp:19-29) along x */
+    for (int r = 0; r < 3; ++r) vds += AT(X, C->VEL + r, c) * SG(r, 0);
+    AT(X, C->E, c) += dt * inv_r * (AT(X, C->E, c) * u - vds);
+    if (s->p.solid) {
+        for (int r = 0; r < 3; ++r)
+            for (int q = 0; q < 3; ++q) {
+                double* v = &AT(X, C->V + 3 * r + q, c);
+                const double g = (r < 2) ? (1.0 / 3.0) * *v * u : -(2.0 / 3.0) * *v * u;
+                *v += dt * inv_r * g;
+            }
+        if (s->p.plastic)
+            for (int m = 0; m < M; ++m) AT(X, C->ARE + m, c) += dt * inv_r * (AT(X, C->ARE + m, c) * u);
+    }
+#undef SG
+}
+
 int tjp_run(tjp_sim* s, double final_t, int max_steps, double* dts, double* t_out)
 {
     const cmap* C = &s->c;
@@ -1317,6 +1352,13 @@ int tjp_run(tjp_sim* s, double final_t, int max_steps, double* dts, double* t_ou
                 }
             }
             if (perr) { *t_out = t; return perr; }
+            if (s->p.radial) { /* geometricSourceTerm (radial.cpp:37-54, main.cpp:159-161) */
+#pragma omp parallel for schedule(static)
+                for (long c = 0; c < N; ++c) {
+                    radial_cell(s, D, D->U1, N, c, dt);
+                    c2p(s, D->U1, N, c);
+                }
+            }
             if (s->p.solid) {
 #pragma omp parallel for schedule(static)
                 for (long c = 0; c < N; ++c) cleanup_v_cell(s, D->U1, N, c);

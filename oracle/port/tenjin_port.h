@@ -30,6 +30,7 @@ typedef struct {
     int eos[TJP_MAX_MAT];   /* 0 MieGruneisen, 1 Romenskii, 2 Wilkins, 3 Hugoniot */
     double eos_params[TJP_MAX_MAT][TJP_MAX_PARAMS];
     double yield_stress[TJP_MAX_MAT];
+    int radial; /* RADIAL: geometric source term (radial.cpp) after plasticUpdate */
 } tjp_params;
 
 typedef struct tjp_sim tjp_sim;

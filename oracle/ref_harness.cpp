@@ -94,6 +94,8 @@ struct Reader {
         if (!f) { std::fprintf(stderr, "cannot open %s\n", path); std::exit(2); }
     }
     int32_t i32() { int32_t v; f.read((char*)&v, 4); return v; }
+    // optional trailing word: `dflt` when the file ends first
+    int32_t i32_or(int32_t dflt) { int32_t v; return f.read((char*)&v, 4) ? v : dflt; }
     double f64() { double v; f.read((char*)&v, 8); return v; }
     void arr(double* p, size_t n) { f.read((char*)p, 8 * n); }
 };
@@ -163,6 +165,7 @@ int main(int argc, char** argv)
         D.prim.assign(nprim, std::vector<double>(nc));
         for (int q = 0; q < nprim; ++q) rd.arr(D.prim[q].data(), nc);
     }
+    const int RADIAL = rd.i32_or(0);  // trailer: RADIAL flag
 
     PlasticEOS plastic;
     plastic.yieldStress.assign(M, 0.0);
@@ -185,7 +188,7 @@ int main(int argc, char** argv)
         Sim& S = sims[di];
         Domain& D = doms[di];
         ParameterStruct& Prm = S.parameters;
-        Prm.SOLID = SOLID; Prm.THINC = THINC; Prm.RADIAL = 0; Prm.PLASTIC = PLASTIC; Prm.REACTIVE = 0; Prm.MUSCL = MUSCL;
+        Prm.SOLID = SOLID; Prm.THINC = THINC; Prm.RADIAL = RADIAL; Prm.PLASTIC = PLASTIC; Prm.REACTIVE = 0; Prm.MUSCL = MUSCL;
         Prm.numberOfMaterials = M; Prm.numberOfMixtures = 0; Prm.Nghost = nghost; Prm.CFL = CFL; Prm.THINCbeta = beta;
         Prm.max_grid_size = 0; Prm.dt = 0.0; Prm.x0 = 0.0;
         for (int d = 0; d < AMREX_SPACEDIM; ++d) { Prm.n_cells[d] = D.n_cells[d]; Prm.dimL[d] = D.dimL[d]; }
@@ -274,6 +277,7 @@ int main(int argc, char** argv)
             advance(*S.U, *S.U1, *S.U2, *S.UL, *S.UR, *S.MUSCLgrad, *S.ULStar, *S.URStar, *S.UStarStar, S.flux_arr,
                     S.geom, Prm, S.bc, *S.THINCArr);
             if (Prm.PLASTIC) plastic.plasticUpdate(*S.U1, Prm);
+            if (Prm.RADIAL) geometricSourceTerm(*S.U1, Prm);
             if (Prm.SOLID) S.U1->cleanUpV();
             S.U1->cleanUpAlpha();
             if (S.U1->contains_nan()) nan_stop = true;

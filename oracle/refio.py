@@ -52,6 +52,7 @@ def write_input(case, path: str) -> None:
                 w(struct.pack("<6i", *b))
             assert d.prim.shape[0] == case.nprim
             w(np.ascontiguousarray(d.prim, dtype="<f8").tobytes())
+        w(struct.pack("<i", int(getattr(case, "radial", 0))))
 
 
 def read_output(case, path: str):

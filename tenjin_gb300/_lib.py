@@ -63,6 +63,7 @@ SIGNATURES = [
     ("tj_compute_dt", _I, [_P, _PD]),
     ("tj_advance", _I, [_P, _D]),
     ("tj_plastic_update", _I, [_P, _D]),
+    ("tj_geometric_source", _I, [_P, _D]),
     ("tj_cleanup_v", _I, [_P]),
     ("tj_cleanup_alpha", _I, [_P]),
     ("tj_cons_to_prim", _I, [_P]),

@@ -70,6 +70,7 @@ class Case:
     thinc: int = 0
     plastic: int = 0
     muscl: int = 1
+    radial: int = 0               # RADIAL: geometric source term, x the radius
     nghost: int = 2
     lo_bc: List[int] = dataclasses.field(default_factory=lambda: [0, 0, 0])
     hi_bc: List[int] = dataclasses.field(default_factory=lambda: [0, 0, 0])

@@ -547,6 +547,7 @@ const char* adj_unsupported(const DevParams& P, int ndom)
 {
     if (P.dim != 2) return "the adjoint covers 2-D domains";
     if (P.solid || P.plastic) return "the adjoint covers fluids";
+    if (P.radial) return "the adjoint covers planar geometry (RADIAL = 0)";
     if (P.M > tja::MM) return "the adjoint covers up to 4 materials";
     for (int m = 0; m < P.M; ++m)
         if (P.eos[m] != TJ_EOS_MIEGRUNEISEN) return "the adjoint covers the stiffened-gas Mie-Gruneisen EOS";

@@ -151,6 +151,7 @@ void make_layouts(const tj_params& p, DevParams& P)
     P.plastic = p.PLASTIC;
     P.muscl = p.MUSCL;
     P.fused64 = p.precision == TJ_PRECISION_FUSED64;
+    P.radial = p.RADIAL ? 1 : 0;
     P.S_ELO = -1;
     for (int d = 0; d < 3; ++d) { P.lo_bc[d] = p.lo_bc[d]; P.hi_bc[d] = p.hi_bc[d]; }
     P.cfl = p.CFL;
@@ -410,7 +411,10 @@ int tj_create(const tj_params* p, tj_ctx** out)
     if (p->dim < 1 || p->dim > 3) return bad("dim must be 1, 2 or 3");
     if (p->n_materials < 1 || p->n_materials > TJ_MAX_MATERIALS) return bad("n_materials out of range");
     if (p->n_mixtures != 0) return bad("mixtures (MixtureEOS) are not supported");
-    if (p->RADIAL || p->REACTIVE) return bad("RADIAL and REACTIVE are not supported");
+    if (p->REACTIVE) return bad("REACTIVE is not supported");
+    if (p->RADIAL && p->SOLID && !p->PLASTIC)
+        return bad("RADIAL with elastic solids is not supported: the source term reads the RK2-averaged stress "
+                   "(hllc.cpp:705, radial.cpp:23), which the carried state does not hold");
     if (p->nghost < 2) return bad("nghost must be >= 2");
     if (p->THINC && p->dim == 3) return bad("THINC is 1-D/2-D only in the reference (thinc.cpp:116-127)");
     if (p->THINC && !p->MUSCL) return bad("THINC needs MUSCL");
@@ -709,13 +713,13 @@ int tj_advance(tj_ctx* c, double dt)
     return check_status(c);
 }
 
-static int cell_op(tj_ctx* c, int op)
+static int cell_op(tj_ctx* c, int op, double dt = 0.0)
 {
     int e = need_state(c);
     if (e) return e;
     Fp64Bufs b = bufs(c);
     a_sync(c);
-    c->launches += fp64_cell_op(c->P, b, c->A, nullptr, op, c->stream);
+    c->launches += fp64_cell_op(c->P, b, c->A, nullptr, op, c->stream, dt);
     if (op != OP_NAN) a_written(c);
     TJ_CUDA(c, cudaGetLastError());
     return check_status(c);
@@ -727,6 +731,12 @@ int tj_plastic_update(tj_ctx* c, double dt)
     if (!c) return TJ_ERR_ARG;
     if (!c->P.plastic) return TJ_OK;
     return cell_op(c, OP_PLASTIC);
+}
+int tj_geometric_source(tj_ctx* c, double dt)
+{
+    if (!c) return TJ_ERR_ARG;
+    if (!(dt >= 0.0)) return fail(c, TJ_ERR_ARG, "tj_geometric_source: dt must be >= 0");
+    return cell_op(c, OP_RADIAL, dt);
 }
 int tj_cleanup_v(tj_ctx* c) { return c ? (c->P.solid ? cell_op(c, OP_CLEAN_V) : TJ_OK) : TJ_ERR_ARG; }
 int tj_cleanup_alpha(tj_ctx* c) { return c ? cell_op(c, OP_CLEAN_ALPHA) : TJ_ERR_ARG; }

@@ -209,6 +209,7 @@ DevParams32 make_params32(const DevParams& DP)
     P.plastic = DP.plastic;
     P.muscl = DP.muscl;
     P.any_solid = DP.any_solid;
+    P.radial = DP.radial;
     for (int d = 0; d < 3; ++d) {
         P.lo_bc[d] = DP.lo_bc[d];
         P.hi_bc[d] = DP.hi_bc[d];

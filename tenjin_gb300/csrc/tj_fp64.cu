@@ -69,7 +69,7 @@ __global__ void k_set_dt(DevScalars* s, double dt)
 // ---------------------------------------------------------------------------
 // Whole-array cell operators of the C ABI.
 // ---------------------------------------------------------------------------
-__global__ void k_cell_op(DevParams P, Fp64Bufs b, double* X, const double* X2, int op)
+__global__ void k_cell_op(DevParams P, Fp64Bufs b, double* X, const double* X2, int op, double dt)
 {
     const long long nt = b.ntot;
     for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < nt; g += (long long)gridDim.x * blockDim.x) {
@@ -90,6 +90,18 @@ __global__ void k_cell_op(DevParams P, Fp64Bufs b, double* X, const double* X2, 
             case OP_PLASTIC: {
                 int e = plastic_cell(P, c);
                 if (e) set_status(b.scal, e);
+                c2p(P, c);
+                break;
+            }
+            case OP_RADIAL: {
+                // geometricSourceTerm (radial.cpp:37-54) with the stress of
+                // the state as its last conservativeToPrimitive left it
+                const DevDomain D = b.doms[find_dom(b.doms, b.ndom, g)];
+                hencky(P, c);
+                stress(P, c);
+                double sg[9];
+                for (int q = 0; q < 9; ++q) sg[q] = c.sigma[q];
+                radial_source(P, c, sg, (int)((g - D.off) % D.n[0]), D.dx[0], dt);
                 c2p(P, c);
                 break;
             }
@@ -267,9 +279,9 @@ int fp64_set_dt(const Fp64Bufs& b, double dt, cudaStream_t st)
     return 1;
 }
 
-int fp64_cell_op(const DevParams& P, const Fp64Bufs& b, double* X, const double* X2, int op, cudaStream_t st)
+int fp64_cell_op(const DevParams& P, const Fp64Bufs& b, double* X, const double* X2, int op, cudaStream_t st, double dt)
 {
-    k_cell_op<<<nblocks(b.ntot), kThreads, 0, st>>>(P, b, X, X2, op);
+    k_cell_op<<<nblocks(b.ntot), kThreads, 0, st>>>(P, b, X, X2, op, dt);
     return 1;
 }
 

@@ -40,8 +40,10 @@ int fp64_step_end(const Fp64Bufs& b, cudaStream_t st);
 int fp64_set_dt(const Fp64Bufs& b, double dt, cudaStream_t st);
 
 // Whole-array operators of the C ABI.
-enum CellOp { OP_C2P = 0, OP_P2C = 1, OP_CLEAN_ALPHA = 2, OP_CLEAN_V = 3, OP_PLASTIC = 4, OP_NAN = 5, OP_AVERAGE = 6 };
-int fp64_cell_op(const DevParams& P, const Fp64Bufs& b, double* X, const double* X2, int op, cudaStream_t st);
+enum CellOp { OP_C2P = 0, OP_P2C = 1, OP_CLEAN_ALPHA = 2, OP_CLEAN_V = 3, OP_PLASTIC = 4, OP_NAN = 5, OP_AVERAGE = 6,
+              OP_RADIAL = 7 };
+int fp64_cell_op(const DevParams& P, const Fp64Bufs& b, double* X, const double* X2, int op, cudaStream_t st,
+                 double dt = 0.0);
 
 // Layout conversion: AccessPattern blocks (valid cells of one box of one
 // domain, ncomp x box cells, i fastest) <-> carried state.

@@ -1186,7 +1186,7 @@ struct MixedImpl : MixedBase {
 // The fused 2-D kernels: one 2-D fluid domain with the stiffened-gas EOS.
 static bool fused2d_covers(const DevParams& DP, size_t ndom)
 {
-    if (DP.dim != 2 || DP.solid || DP.plastic || ndom != 1 || DP.M > 4) return false;
+    if (DP.dim != 2 || DP.solid || DP.plastic || DP.radial || ndom != 1 || DP.M > 4) return false;
     for (int m = 0; m < DP.M; ++m)
         if (DP.eos[m] != TJ_EOS_MIEGRUNEISEN || DP.phase[m] != TJ_PHASE_FLUID) return false;
     return true;
@@ -1195,7 +1195,7 @@ static bool fused2d_covers(const DevParams& DP, size_t ndom)
 // The fused 3-D kernel: 3-D fluids with the stiffened-gas EOS, MUSCL (no THINC).
 static bool fused3d_covers(const DevParams& DP)
 {
-    if (DP.dim != 3 || DP.solid || DP.plastic || DP.thinc || DP.M > 4) return false;
+    if (DP.dim != 3 || DP.solid || DP.plastic || DP.thinc || DP.radial || DP.M > 4) return false;
     for (int m = 0; m < DP.M; ++m)
         if (DP.eos[m] != TJ_EOS_MIEGRUNEISEN || DP.phase[m] != TJ_PHASE_FLUID) return false;
     return true;
@@ -1206,7 +1206,7 @@ bool mixed_supported(const tj_params& p)
     // binary32: every configuration (fused kernels where they apply, the
     // binary32 per-direction kernels otherwise); binary64 fused: 2-D fluids
     if (p.precision == TJ_PRECISION_MIXED) return true;
-    if (p.dim != 2 || p.SOLID || p.PLASTIC) return false;
+    if (p.dim != 2 || p.SOLID || p.PLASTIC || p.RADIAL) return false;
     if (p.n_materials < 1 || p.n_materials > 4) return false;
     for (int m = 0; m < p.n_materials; ++m)
         if (p.materials[m].eos != TJ_EOS_MIEGRUNEISEN || p.materials[m].phase != TJ_PHASE_FLUID) return false;

@@ -841,6 +841,41 @@ __device__ inline bool cell_has_nan(const PT& P, const CellT<R>& c)
     return n;
 }
 
+// addGeometricSourceTerm (radial.cpp:5-31) on one cell: every conservative
+// variable gains dt * (multiplier / r) * geometricFlux (flux.cpp:51-77), with
+// r = (i + 0.5) dx[0] and multiplier -2 in 1-D (spherical symmetry), -1 in 2-D
+// and 3-D (cylindrical). `sg` is the stress the reference's state holds at that
+// point and the velocity is the cell's; neither changes while the conservative
+// variables are updated, so the per-cell order is the reference's.
+template <typename PT, typename R = typename PT::real>
+__device__ inline void radial_source(const PT& P, CellT<R>& c, const R* sg, int i, double dx0, R dt)
+{
+    const R inv_r = R(P.dim == 1 ? -2.0 : -1.0) / (((R)i + R(0.5)) * (R)dx0);
+    const R s = dt * inv_r;
+    const R u = c.vel[0];
+    for (int m = 0; m < P.M; ++m) {
+        c.alpha[m] += s * R(0.0);
+        c.arho[m] += s * (c.arho[m] * u);
+    }
+    c.rhou[0] += s * (((c.rhou[0] * u) - sg[0]) + sg[8]);
+    c.rhou[1] += s * ((c.rhou[1] * u) - sg[1]);
+    c.rhou[2] += s * (R(-2.0) * sg[2]);
+    R vds = R(0.0);  // vdotsigma (flux.cpp:19-29) along x
+#pragma unroll
+    for (int r = 0; r < 3; ++r) vds += c.vel[r] * sg[3 * r];
+    if constexpr (sizeof(R) == 4) dd_add32(c.E, c.Elo, s * ((c.E * u) - vds));
+    else c.E += s * ((c.E * u) - vds);
+    if (P.solid) {
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+            const R g = (q < 6) ? (R(1.0) / R(3.0)) * c.V[q] * u : -(R(2.0) / R(3.0)) * c.V[q] * u;
+            c.V[q] += s * g;
+        }
+        if (P.plastic)
+            for (int m = 0; m < P.M; ++m) c.are[m] += s * (c.are[m] * u);
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Update of one direction; last direction: c2p; second stage: average and
 // the post-advance operators of main.cpp:145-187.
@@ -890,6 +925,7 @@ __global__ void k_update(PT P, PathBufs<typename PT::real> b, const R* __restric
         if (last) {
             c2p(P, Yc);
             if (finish) {
+                const R p_stage = Yc.p;  // U2's pressure, before the average
                 // U1 = U*0.5 + U2*0.5 over every carried component (hllc.cpp:705)
                 CellT<R> A0;
                 load_state(P, b.A, nt, g, nullptr, A0);
@@ -928,6 +964,23 @@ __global__ void k_update(PT P, PathBufs<typename PT::real> b, const R* __restric
                         c2p(P, Yc);
                     }
                     if (e) set_status(b.scal, e);
+                }
+                if (P.radial) {
+                    // the stress the reference's U1 holds here: fresh from the
+                    // plastic update's c2p, else the average of U's and U2's
+                    // (fluids only: -p I each, boxaccesscellarray.cpp:204-212)
+                    R sg[9];
+#pragma unroll
+                    for (int r = 0; r < 3; ++r)
+#pragma unroll
+                        for (int qq = 0; qq < 3; ++qq) {
+                            const R dl = (R)(r == qq);
+                            sg[3 * r + qq] = P.plastic ? Yc.sigma[3 * r + qq]
+                                                       : ((-A0.p * dl) * (R(1.0) / R(2.0))) +
+                                                             ((-p_stage * dl) * (R(1.0) / R(2.0)));
+                        }
+                    radial_source(P, Yc, sg, i, D.dx[0], dtdx_num);
+                    c2p(P, Yc);  // geometricSourceTerm (radial.cpp:50)
                 }
                 if (P.solid) cleanup_v_cell(P, Yc);
                 int e = cleanup_alpha(P, Yc.alpha);

@@ -13,6 +13,7 @@ struct DevParams {
     using real = double;
     int dim, M, solid, thinc, plastic, muscl, any_solid;
     int fused64;  // fused kernels in binary64 (TJ_PRECISION_FUSED64)
+    int radial;   // RADIAL: geometric source term after the plastic update
     int lo_bc[3], hi_bc[3];
     double cfl, beta;
     int phase[TJ_MAX_MAT], eos[TJ_MAX_MAT];
@@ -37,6 +38,7 @@ struct DevParams32 {
     using real = float;
     int dim, M, solid, thinc, plastic, muscl, any_solid;
     int fused64;
+    int radial;
     int lo_bc[3], hi_bc[3];
     float cfl, beta;
     int phase[TJ_MAX_MAT], eos[TJ_MAX_MAT];

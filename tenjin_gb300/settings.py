@@ -185,10 +185,11 @@ def to_case(cfg: Dict[str, Any], dim: int, max_grid_size: int,
     M = len(mats)
     c = Case("settings", dim, mats, solid=int(cfg.get("SOLID", 0)), thinc=int(cfg.get("THINC", 0)),
              plastic=int(cfg.get("PLASTIC", 0)), muscl=int(cfg.get("MUSCL", 1)), nghost=nghost,
+             radial=int(cfg.get("RADIAL", 0)),
              cfl=float(cfg["CFL"]), thinc_beta=float(cfg.get("THINCbeta", 1.6)),
              final_t=float(cfg["finalTime"]))
-    if int(cfg.get("mixtures", 0)) or int(cfg.get("RADIAL", 0)) or int(cfg.get("REACTIVE", 0)):
-        raise SettingsError("mixtures, RADIAL and REACTIVE are not supported")
+    if int(cfg.get("mixtures", 0)) or int(cfg.get("REACTIVE", 0)):
+        raise SettingsError("mixtures and REACTIVE are not supported")
     axes = "xyz"
     n = [int(cfg[f"numberOf{axes[d]}Cells"]) if d < dim else 1 for d in range(3)]
     L = [float(cfg[f"{axes[d]}domainLength"]) if d < dim else 1.0 for d in range(3)]

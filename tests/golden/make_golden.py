@@ -2,7 +2,7 @@
 OWN hot-path sources (compiled from the reference tree through oracle/Makefile
 into oracle/_ref/) on seeded synthetic inputs.
 
-Run where the reference tree exists:  python tests/golden/make_golden.py
+Run where the reference tree exists:  python tests/golden/make_golden.py [name ...]
 Each fixture stores the builder call that makes its input, a SHA-256 of the
 initial primitive fields, the dt of every step and the final values of the
 carried components (AccessPattern indices listed in the file).
@@ -38,6 +38,13 @@ FIXTURES = {
     "wilkins2d_plastic": ("solid_mixture_2d", {"eos": cases.EOS_WILKINS, "n": 20, "max_steps": 10}),
     "romenskii2d_plastic": ("solid_mixture_2d", {"eos": cases.EOS_ROMENSKII, "n": 20, "max_steps": 10}),
     "hugoniot2d_plastic": ("solid_mixture_2d", {"eos": cases.EOS_HUGONIOT, "n": 16, "max_steps": 10}),
+    # RADIAL: x is the radius, a reflective axis at x = 0
+    "sod_spherical_1d": ("sod_1d", {"ncells": 200, "max_grid_size": 64, "max_steps": 80},
+                         {"radial": 1, "lo_bc": [1, 0, 0]}),
+    "bubble_cylindrical": ("shock_bubble_2d", {"n": 40, "max_grid_size": 16, "max_steps": 30, "radius": 0.3},
+                           {"radial": 1, "lo_bc": [1, 1, 0], "hi_bc": [1, 0, 0]}),
+    "wilkins2d_plastic_cylindrical": ("solid_mixture_2d", {"eos": cases.EOS_WILKINS, "n": 20, "max_steps": 10},
+                                      {"radial": 1, "lo_bc": [1, 0, 0]}),
 }
 
 
@@ -56,10 +63,16 @@ def prim_sha(c):
     return h.hexdigest()
 
 
-def main():
+def main(names=None):
+    """Regenerates the named fixtures (all when none are named); the manifest
+    keeps the entries of the others."""
     subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "-j3"], check=True)
     manifest = {}
-    for name in FIXTURES:
+    mpath = os.path.join(HERE, "manifest.json")
+    if names and os.path.exists(mpath):
+        with open(mpath) as f:
+            manifest = json.load(f)["fixtures"]
+    for name in (names or FIXTURES):
         c = build_case(name)
         out = refio.run_reference(c)
         if out["nan_stop"]:
@@ -79,4 +92,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

@@ -62,3 +62,20 @@ def test_several_2d_domains_with_thinc():
     l1, _, cfg = compare(c, 40)
     assert "binary32 per-direction" in cfg
     assert l1 <= L1_TOL, l1
+
+
+@pytest.mark.parametrize("geom", ["spherical_1d", "cylindrical_2d", "cylindrical_plastic"])
+def test_radial_source(geom):
+    if geom == "spherical_1d":
+        c = cases.sod_1d(ncells=400, max_grid_size=100, max_steps=300)
+        c.lo_bc = [1, 0, 0]
+    elif geom == "cylindrical_2d":
+        c = cases.shock_bubble_2d(n=48, max_grid_size=24, max_steps=60, radius=0.3)
+        c.lo_bc, c.hi_bc = [1, 1, 0], [1, 0, 0]
+    else:
+        c = cases.solid_mixture_2d(eos=cases.EOS_WILKINS, n=24, max_steps=10)
+        c.lo_bc = [1, 0, 0]
+    c.radial = 1
+    l1, _, cfg = compare(c, c.max_steps)
+    assert "binary32 per-direction" in cfg
+    assert l1 <= L1_TOL, l1

@@ -74,6 +74,31 @@ def test_operators_match_port_one_by_one():
     assert fx.rel_diff(g.state(0)[idx], ref["states"][0][idx]) <= TOL
 
 
+@pytest.mark.parametrize("name", ["sod_spherical_1d", "wilkins2d_plastic_cylindrical"])
+def test_radial_operators_one_by_one(name):
+    """The loop of main.cpp:121-191 with RADIAL driven from the host:
+    getTimeStep, advance, plasticUpdate, geometricSourceTerm, cleanUpV,
+    cleanUpAlpha, against the fused steps of the port."""
+    c = fx.build_case(name)
+    c.max_steps = 6
+    g = TenjinGPU(c)
+    ref = port.run_port(c)
+    for n in range(c.max_steps):
+        dt = g.getTimeStep()
+        if n < 5:
+            dt *= 0.2
+        assert abs(dt - ref["dts"][n]) <= TOL * dt
+        g.advance(dt)
+        if c.plastic:
+            g.plasticUpdate(dt)
+        g.geometricSourceTerm(dt)
+        if c.solid:
+            g.cleanUpV()
+        g.cleanUpAlpha()
+    idx = carried_components(c)
+    assert fx.rel_diff(g.state(0)[idx], ref["states"][0][idx]) <= TOL
+
+
 def test_fab_exchange_roundtrip_keeps_ghosts():
     c = cases.shock_bubble_2d(n=24, max_grid_size=10, max_steps=1)
     g = TenjinGPU(c)

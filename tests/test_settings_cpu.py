@@ -62,9 +62,16 @@ def test_to_case_maps_keys_and_applies_the_pressure_correction():
     assert np.all(d.prim[0, 0, 0, :50] == a0) and np.all(d.prim[0, 0, 0, 50:] == a1)
 
 
-def test_to_case_rejects_what_the_path_does_not_cover():
+def test_to_case_carries_radial():
     cfg = settings.parse(DECK)
     cfg["RADIAL"] = 1
+    assert settings.to_case(cfg, 1, 50).radial == 1
+    assert settings.to_case(settings.parse(DECK), 1, 50).radial == 0
+
+
+def test_to_case_rejects_what_the_path_does_not_cover():
+    cfg = settings.parse(DECK)
+    cfg["REACTIVE"] = 1
     with pytest.raises(settings.SettingsError):
         settings.to_case(cfg, 1, 50)
     cfg = settings.parse(DECK)
