@@ -30,7 +30,7 @@ class _Params(ctypes.Structure):
         ("phase", ctypes.c_int * MAX_MAT), ("eos", ctypes.c_int * MAX_MAT),
         ("eos_params", (ctypes.c_double * MAX_PARAMS) * MAX_MAT),
         ("yield_stress", ctypes.c_double * MAX_MAT),
-        ("radial", ctypes.c_int),
+        ("radial", ctypes.c_int), ("nmix", ctypes.c_int), ("reactive", ctypes.c_int),
     ]
 
 
@@ -88,6 +88,8 @@ def make_params(case) -> _Params:
         p.lo_bc[d], p.hi_bc[d] = case.lo_bc[d], case.hi_bc[d]
     p.cfl, p.thinc_beta = case.cfl, case.thinc_beta
     p.radial = getattr(case, "radial", 0)
+    p.nmix = getattr(case, "nmix", 0)
+    p.reactive = getattr(case, "reactive", 0)
     for m, mat in enumerate(case.materials):
         p.phase[m], p.eos[m] = mat.phase, mat.eos
         for q, v in enumerate(mat.params):

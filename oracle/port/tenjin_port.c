@@ -20,6 +20,7 @@
 typedef struct {
     int ALPHA, ALPHARHO, RHO_K, RHO, RHOU, VEL, E, P, A, USTAR, SIGMA;
     int V, VSTAR, DEVH, HJ2, EPS, ARE;
+    int RMIX, LAM, ARL; /* mixture: rhomix (2), lambda, alpharholambda; -1 without */
     int ncomp;
 } cmap;
 
@@ -38,6 +39,12 @@ static cmap make_cmap(const tjp_params* p)
     c.A = n; n += 1;
     c.USTAR = n; n += 1;
     c.SIGMA = n; n += 9;
+    c.RMIX = c.LAM = c.ARL = -1;
+    if (p->nmix) {
+        c.RMIX = n; n += 2;
+        c.LAM = n; n += 1;
+        c.ARL = n; n += 1;
+    }
     c.V = c.VSTAR = c.DEVH = c.HJ2 = c.EPS = c.ARE = -1;
     if (p->solid) {
         c.V = n; n += 9;
@@ -263,16 +270,29 @@ static void sqrtm3(const double* A, double* R)
 /* ------------------------------------------------------------------------ */
 typedef struct {
     double alpha, arho, rhok, p, hj2;
+    double lam, rm0, rm1; /* MixtureEOS only: lambda, rhomix rows 0 and 1 */
 } ecell;
 
 static double Gam(const tjp_sim* s, int m) { return s->p.eos_params[m][0] - 1.0; }
 #define PRM(m, q) (s->p.eos_params[m][q])
+
+/* MixtureEOS (equationofstate.cpp:117-396): two stiffened gases
+ * [gamma, pref, eref, CV] x 2 blended by lambda; GruneisenGamma = gamma - 1. */
+#define MG1(m) (PRM(m, 0) - 1.0)
+#define MG2(m) (PRM(m, 4) - 1.0)
+static double mix_gamma_term(const tjp_sim* s, int m, double lam) /* :175, :224 */
+{
+    return (lam * PRM(m, 0) * PRM(m, 3) + (1.0 - lam) * PRM(m, 4) * PRM(m, 7)) / (lam * PRM(m, 3) + (1.0 - lam) * PRM(m, 7)) -
+           1.0;
+}
 
 static double eos_e_cold(const tjp_sim* s, int m, const ecell* e)
 {
     double x;
     switch (s->p.eos[m]) {
         case 0: return PRM(m, 2) * e->arho; /* equationofstate.cpp:37-40 */
+        case 4: /* :161-165 */
+            return e->lam * (PRM(m, 2) * e->arho) + (1.0 - e->lam) * (PRM(m, 6) * e->arho);
         case 1: {
             double a = PRM(m, 6), K0 = PRM(m, 5), r0 = PRM(m, 4);
             x = e->rhok / r0;
@@ -297,6 +317,9 @@ static double eos_p_cold(const tjp_sim* s, int m, const ecell* e)
     double G = Gam(s, m), x;
     switch (s->p.eos[m]) {
         case 0: return PRM(m, 1) * e->alpha / G; /* equationofstate.cpp:42-45 */
+        case 4: /* :167-171 */
+            return (PRM(m, 1) * e->alpha / MG1(m)) * e->lam * e->rhok / (e->rm0) +
+                   (PRM(m, 5) * e->alpha / MG2(m)) * (1.0 - e->lam) * e->rhok / (e->rm1);
         case 1: {
             double a = PRM(m, 6), K0 = PRM(m, 5), r0 = PRM(m, 4);
             x = e->rhok / r0;
@@ -320,6 +343,7 @@ static double eos_G(const tjp_sim* s, int m, const ecell* e)
 {
     switch (s->p.eos[m]) {
         case 0: return 0.0 * e->alpha;
+        case 4: return 0.0;
         case 1: return PRM(m, 8) * tjm_pow((e->rhok / PRM(m, 4)), PRM(m, 7) + 1.0);
         case 2: return PRM(m, 10);
         default: return PRM(m, 7);
@@ -354,6 +378,7 @@ static double eos_e_shear(const tjp_sim* s, int m, const ecell* e)
 {
     switch (s->p.eos[m]) {
         case 0: return 0.0 * e->alpha;
+        case 4: return 0.0;
         case 3: return e->alpha * (PRM(m, 7) * e->hj2);
         default: return e->alpha * (eos_G(s, m, e) * e->hj2);
     }
@@ -364,18 +389,36 @@ static double eos_p_shear(const tjp_sim* s, int m, const ecell* e)
     double G = Gam(s, m);
     switch (s->p.eos[m]) {
         case 0: return 0.0 * e->alpha;
+        case 4: return 0.0;
         case 3: return (e->alpha / G) * ((e->rhok * 0.0 - PRM(m, 7)) * e->hj2);
         default: return (e->alpha / G) * ((e->rhok * eos_dGdrho(s, m, e) - eos_G(s, m, e)) * e->hj2);
     }
 }
 
-static double eos_invG(const tjp_sim* s, int m, const ecell* e) { return e->alpha / Gam(s, m); }
+static double eos_invG(const tjp_sim* s, int m, const ecell* e)
+{
+    if (s->p.eos[m] == 4) return e->alpha / mix_gamma_term(s, m, e->lam); /* :173-178 */
+    return e->alpha / Gam(s, m);
+}
+
+/* xi (equationofstate.cpp:72-75, 222-225) */
+static double eos_xi(const tjp_sim* s, int m, const ecell* e)
+{
+    if (s->p.eos[m] == 4) return 1.0 / mix_gamma_term(s, m, e->lam);
+    return 1.0 / Gam(s, m);
+}
 
 static double eos_c2(const tjp_sim* s, int m, const ecell* e)
 {
     double G = Gam(s, m);
     switch (s->p.eos[m]) {
         case 0: return e->p * (G + 1.0) / e->rhok - PRM(m, 1) / e->rhok; /* :61-64 */
+        case 4: { /* mixtureSoundSpeed (:208-220) */
+            double dedrho = (e->lam) * ((PRM(m, 1) - e->p) / (MG1(m) * e->rhok * e->rhok));
+            dedrho += (1.0 - e->lam) * ((PRM(m, 5) - e->p) / (MG2(m) * e->rhok * e->rhok));
+            return (e->p / (e->rhok * e->rhok) - dedrho) /
+                   (e->lam / (e->rm0 * MG1(m)) + (1.0 - e->lam) / (e->rm1 * MG2(m)));
+        }
         case 1: {
             double a = PRM(m, 6), K0 = PRM(m, 5), r0 = PRM(m, 4), x = e->rhok / r0;
             double dpc = (K0 / (a * r0)) * tjm_pow(x, a) * ((2.0 * a + 1.0) * tjm_pow(x, a) - (a + 1.0));
@@ -414,6 +457,12 @@ static void cell_ecell(const tjp_sim* s, const double* X, long N, long c, int m,
     e->rhok = AT(X, C->RHO_K + m, c);
     e->p = AT(X, C->P, c);
     e->hj2 = C->HJ2 >= 0 ? AT(X, C->HJ2, c) : 0.0;
+    e->lam = e->rm0 = e->rm1 = 0.0;
+    if (s->p.eos[m] == 4) {
+        e->lam = AT(X, C->LAM, c);
+        e->rm0 = AT(X, C->RMIX, c);
+        e->rm1 = AT(X, C->RMIX + 1, c);
+    }
 }
 
 static double eff_invG(const tjp_sim* s, const double* X, long N, long c) /* :218-228 */
@@ -492,6 +541,72 @@ static void stress(const tjp_sim* s, double* X, long N, long c)
         }
 }
 
+/* MixtureEOS root finding (equationofstate.cpp:238-376) for material 0:
+ * the mixture densities at which the two components' temperatures agree. */
+static double mix_rhob(const tjp_sim* s, double* X, long N, long c, double rhoa) /* rhobFunc :243-246 */
+{
+    const cmap* C = &s->c;
+    return (1.0 - AT(X, C->LAM, c)) / (1.0 / AT(X, C->RHO_K, c) - AT(X, C->LAM, c) / rhoa);
+}
+
+static double mix_bisection(const tjp_sim* s, double* X, long N, long c, double rhoTry, double ke) /* :262-272 */
+{
+    const cmap* C = &s->c;
+    AT(X, C->RMIX, c) = rhoTry;
+    AT(X, C->RMIX + 1, c) = mix_rhob(s, X, N, c, rhoTry);
+    double p = (AT(X, C->E, c) - ke - eff_e_nonthermal(s, X, N, c) + eff_p_nonthermal(s, X, N, c)) / (eff_invG(s, X, N, c));
+    /* pressureFunction (:251-260) */
+    return ((p - PRM(0, 1)) / (AT(X, C->RMIX, c) * MG1(0) * PRM(0, 3))) -
+           ((p - PRM(0, 5)) / (AT(X, C->RMIX + 1, c) * MG2(0) * PRM(0, 7)));
+}
+
+static int sgn_d(double v) { return (0.0 < v) - (v < 0.0); }
+
+static void mix_root_find(tjp_sim* s, double* X, long N, long c, double ke) /* rootFind :274-376 */
+{
+    const cmap* C = &s->c;
+    const double lam = AT(X, C->LAM, c), rk = AT(X, C->RHO_K, c);
+    if (PRM(0, 1) == 0.0 && PRM(0, 5) == 0.0) {
+        AT(X, C->RMIX, c) = rk * (lam + (1.0 - lam) * (MG2(0) * PRM(0, 7)) / (MG1(0) * PRM(0, 3)));
+        AT(X, C->RMIX + 1, c) = mix_rhob(s, X, N, c, AT(X, C->RMIX, c));
+        return;
+    }
+    if (lam > 1.0 - 1E-3) {
+        AT(X, C->RMIX, c) = rk;
+        AT(X, C->RMIX + 1, c) = rk;
+        return;
+    } else if (lam < 1E-3) {
+        AT(X, C->RMIX + 1, c) = rk;
+        AT(X, C->RMIX, c) = rk;
+        return;
+    }
+    double A = lam * rk + 1E-10, B = 1000000.0;
+    double mid = 0.5 * (A + B);
+    if (fabs(mix_bisection(s, X, N, c, A, ke)) <= 1E-4) {
+        AT(X, C->RMIX, c) = A;
+        AT(X, C->RMIX + 1, c) = mix_rhob(s, X, N, c, AT(X, C->RMIX, c));
+        return;
+    } else if (fabs(mix_bisection(s, X, N, c, B, ke)) <= 1E-4) {
+        AT(X, C->RMIX, c) = B;
+        AT(X, C->RMIX + 1, c) = mix_rhob(s, X, N, c, AT(X, C->RMIX, c));
+        return;
+    }
+    if (sgn_d(mix_bisection(s, X, N, c, A, ke)) == sgn_d(mix_bisection(s, X, N, c, B, ke))) {
+        s->err = -5; /* "Error in root Bisection" and exit(1) in the reference */
+        return;
+    }
+    for (int n = 0;; n++) {
+        if (sgn_d(mix_bisection(s, X, N, c, mid, ke)) == sgn_d(mix_bisection(s, X, N, c, A, ke))) A = mid;
+        else B = mid;
+        mid = 0.5 * (A + B);
+        if (fabs(A - B) / (A + B) < 1E-7) {
+            AT(X, C->RMIX, c) = mid;
+            AT(X, C->RMIX + 1, c) = mix_rhob(s, X, N, c, AT(X, C->RMIX, c));
+            return;
+        }
+    }
+}
+
 /* conservativeToPrimitive (boxaccesscellarray.cpp:67-122) */
 static void c2p(const tjp_sim* s, double* X, long N, long c)
 {
@@ -509,6 +624,10 @@ static void c2p(const tjp_sim* s, double* X, long N, long c)
         AT(X, C->VEL + r, c) = AT(X, C->RHOU + r, c) / AT(X, C->RHO, c);
         ke += 0.5 * AT(X, C->RHO, c) * AT(X, C->VEL + r, c) * AT(X, C->VEL + r, c);
     }
+    if (s->p.nmix) { /* :104-113 */
+        AT(X, C->LAM, c) = AT(X, C->ARL, c) / AT(X, C->ALPHARHO, c);
+        mix_root_find((tjp_sim*)s, X, N, c, ke);
+    }
     AT(X, C->P, c) = (AT(X, C->E, c) - ke - eff_e_nonthermal(s, X, N, c) + eff_p_nonthermal(s, X, N, c)) / (eff_invG(s, X, N, c));
     stress(s, X, N, c);
 }
@@ -522,6 +641,14 @@ static void p2c(const tjp_sim* s, double* X, long N, long c)
     for (int m = 0; m < M; ++m) {
         AT(X, C->ALPHARHO + m, c) = AT(X, C->ALPHA + m, c) * AT(X, C->RHO_K + m, c);
         AT(X, C->RHO, c) += AT(X, C->ALPHARHO + m, c);
+        if (s->p.nmix && m == 0) {
+            AT(X, C->ARL, c) = AT(X, C->LAM, c) * AT(X, C->ALPHA, c) * AT(X, C->RHO_K, c);
+            /* defineMixtureDensities (equationofstate.cpp:390-396) */
+            const double lam = AT(X, C->LAM, c), pp = AT(X, C->P, c);
+            AT(X, C->RMIX, c) = AT(X, C->RHO_K, c) * (lam + (1.0 - lam) * ((pp - PRM(0, 1)) / (pp - PRM(0, 5))) *
+                                                               ((PRM(0, 7) * MG2(0)) / (PRM(0, 3) * MG1(0))));
+            AT(X, C->RMIX + 1, c) = mix_rhob(s, X, N, c, AT(X, C->RMIX, c));
+        }
         if (s->p.plastic && s->p.phase[m] == 0) AT(X, C->ARE + m, c) = AT(X, C->EPS + m, c) * AT(X, C->ALPHARHO + m, c);
     }
     hencky(s, X, N, c);
@@ -542,10 +669,9 @@ static void sound_speed(const tjp_sim* s, double* X, long N, long c)
     for (int m = 0; m < s->p.M; ++m) {
         ecell e;
         cell_ecell(s, X, N, c, m, &e);
-        double xi = 1.0 / Gam(s, m);
-        double v = xi * eos_c2(s, m, &e) * AT(X, C->ALPHARHO + m, c) / AT(X, C->RHO, c);
+        double v = eos_xi(s, m, &e) * eos_c2(s, m, &e) * AT(X, C->ALPHARHO + m, c) / AT(X, C->RHO, c);
         a += (0.0 < v) ? v : 0.0;
-        xit += xi * AT(X, C->ALPHA + m, c);
+        xit += eos_xi(s, m, &e) * AT(X, C->ALPHA + m, c);
     }
     if (a <= 0.0) a = 1E-6;
     AT(X, C->A, c) = sqrt(a / xit);
@@ -608,6 +734,7 @@ static double pflux(const tjp_sim* s, int comp, const double* U, int d) /* flux.
     if (comp >= C->ALPHA && comp < C->ALPHA + s->p.M) return CV(U, comp) * ud;
     if (comp >= C->ALPHARHO && comp < C->ALPHARHO + s->p.M) return CV(U, comp) * ud;
     if (C->ARE >= 0 && comp >= C->ARE && comp < C->ARE + s->p.M) return CV(U, comp) * ud;
+    if (comp == C->ARL) return CV(U, comp) * ud;
     if (comp >= C->RHOU && comp < C->RHOU + 3) return CV(U, comp) * ud - CV(U, C->SIGMA + 3 * (comp - C->RHOU) + d);
     if (comp == C->E) {
         double r = 0.0;
@@ -631,6 +758,7 @@ static void star_state(const tjp_sim* s, const double* U, double* Us, double SK,
         CV(Us, C->ALPHA + m) = CV(U, C->ALPHA + m);
         CV(Us, C->ALPHARHO + m) = mult * CV(U, C->ALPHARHO + m);
         CV(Us, C->RHO_K + m) = CV(Us, C->ALPHARHO + m) / CV(Us, C->ALPHA + m);
+        if (s->p.nmix && m == 0) CV(Us, C->ARL) = mult * CV(U, C->ARL);
         if (s->p.plastic && s->p.phase[m] == 0) CV(Us, C->ARE + m) = mult * CV(U, C->ARE + m);
         CV(Us, C->RHO) += CV(Us, C->ALPHARHO + m);
     }
@@ -659,7 +787,7 @@ static double sstar(const tjp_sim* s, const double* L, const double* R, double S
 }
 
 /* Conservative-variable list (accesspattern.cpp:48-75): alpha, alphaRho, rhoU,
- * E, V, alphaRhoEpsilon. */
+ * E, alphaRhoLambda, V, alphaRhoEpsilon. */
 static int cons_list(const tjp_sim* s, int* out)
 {
     const cmap* C = &s->c;
@@ -668,6 +796,7 @@ static int cons_list(const tjp_sim* s, int* out)
     for (int m = 0; m < s->p.M; ++m) out[n++] = C->ALPHARHO + m;
     for (int r = 0; r < 3; ++r) out[n++] = C->RHOU + r;
     out[n++] = C->E;
+    if (s->p.nmix) out[n++] = C->ARL;
     if (s->p.solid)
         for (int q = 0; q < 9; ++q) out[n++] = C->V + q;
     if (s->p.plastic)
@@ -675,7 +804,7 @@ static int cons_list(const tjp_sim* s, int* out)
     return n;
 }
 
-/* Primitive-variable list: alpha, rho_k, u, p, V, epsilon. */
+/* Primitive-variable list: alpha, rho_k, u, p, lambda, V, epsilon. */
 static int prim_list(const tjp_sim* s, int* out)
 {
     const cmap* C = &s->c;
@@ -684,6 +813,7 @@ static int prim_list(const tjp_sim* s, int* out)
     for (int m = 0; m < s->p.M; ++m) out[n++] = C->RHO_K + m;
     for (int r = 0; r < 3; ++r) out[n++] = C->VEL + r;
     out[n++] = C->P;
+    if (s->p.nmix) out[n++] = C->LAM;
     if (s->p.solid)
         for (int q = 0; q < 9; ++q) out[n++] = C->V + q;
     if (s->p.plastic)
@@ -1246,6 +1376,11 @@ int tjp_set_primitive(tjp_sim* s, int dom, const double* prim)
         for (int r = 0; r < 9; ++r, ++q) memcpy(&AT(D->U1, C->V + r, 0), prim + (size_t)q * N, sizeof(double) * N);
     if (s->p.plastic)
         for (int m = 0; m < M; ++m, ++q) memcpy(&AT(D->U1, C->EPS + m, 0), prim + (size_t)q * N, sizeof(double) * N);
+    if (s->p.nmix) { /* initialise.cpp:66-71 */
+        memcpy(&AT(D->U1, C->LAM, 0), prim + (size_t)q * N, sizeof(double) * N);
+        memcpy(&AT(D->U1, C->RMIX, 0), &AT(D->U1, C->RHO_K, 0), sizeof(double) * N);
+        memcpy(&AT(D->U1, C->RMIX + 1, 0), &AT(D->U1, C->RHO_K, 0), sizeof(double) * N);
+    }
     for (long c = 0; c < N; ++c) p2c(s, D->U1, N, c);
     return 0;
 }
@@ -1303,6 +1438,7 @@ static void radial_cell(tjp_sim* s, const pdom* D, double* X, long N, long c, do
     double vds = 0.0; /* vdotsigma (flux.cpp:19-29) along x */
     for (int r = 0; r < 3; ++r) vds += AT(X, C->VEL + r, c) * SG(r, 0);
     AT(X, C->E, c) += dt * inv_r * (AT(X, C->E, c) * u - vds);
+    if (s->p.nmix) AT(X, C->ARL, c) += dt * inv_r * (AT(X, C->ARL, c) * u);
     if (s->p.solid) {
         for (int r = 0; r < 3; ++r)
             for (int q = 0; q < 3; ++q) {
@@ -1314,6 +1450,30 @@ static void radial_cell(tjp_sim* s, const pdom* D, double* X, long N, long c, do
             for (int m = 0; m < M; ++m) AT(X, C->ARE + m, c) += dt * inv_r * (AT(X, C->ARE + m, c) * u);
     }
 #undef SG
+}
+
+/* pressureBased_UpdateMassFraction (reactive.cpp:3-26) for material 0:
+ * alphaRhoLambda after one explicit Euler step of the pressure-based rate. */
+static double reactive_euler(double arl, double arho, double p, double alpha, double dt)
+{
+    const double sigma = 20.0, nu = 0.5, n = 1.2;
+    if (alpha < 0.5) return arl;
+    double r = arl - (dt) * (sigma * tjm_pow(arho, 1.0 - nu) * tjm_pow(arl, nu) * tjm_pow((p / 1E6), n));
+    if (r < 0.0) r = 0.0;
+    return r;
+}
+
+/* reactiveUpdate (reactive.cpp:60-103) on one cell: two Euler steps from the
+ * same alphaRho, pressure and alpha, averaged with the start value, then
+ * conservativeToPrimitive. */
+static void reactive_cell(tjp_sim* s, double* X, long N, long c, double dt)
+{
+    const cmap* C = &s->c;
+    const double a0 = AT(X, C->ARL, c), arho = AT(X, C->ALPHARHO, c), p = AT(X, C->P, c), al = AT(X, C->ALPHA, c);
+    const double a1 = reactive_euler(a0, arho, p, al, dt);
+    const double a2 = reactive_euler(a1, arho, p, al, dt);
+    AT(X, C->ARL, c) = ((a0 * (1.0 / 2.0)) + (a2 * (1.0 / 2.0)));
+    c2p(s, X, N, c);
 }
 
 int tjp_run(tjp_sim* s, double final_t, int max_steps, double* dts, double* t_out)
@@ -1337,11 +1497,18 @@ int tjp_run(tjp_sim* s, double final_t, int max_steps, double* dts, double* t_ou
             long N = D->N;
             memcpy(D->U, D->U1, sizeof(double) * nc * N);
             int e = stage(s, D, D->U, D->U1, dt);
+            if (!e) e = s->err;
             if (!e) e = stage(s, D, D->U1, D->U2, dt);
+            if (!e) e = s->err;
             if (e) { *t_out = t; return e; }
             /* U1 = U*0.5 + U2*0.5 over every component (hllc.cpp:705) */
 #pragma omp parallel for schedule(static)
             for (long x = 0; x < (long)nc * N; ++x) D->U1[x] = (D->U[x] * (1.0 / 2.0)) + (D->U2[x] * (1.0 / 2.0));
+            if (s->p.reactive && s->p.nmix) { /* main.cpp:149-152 */
+#pragma omp parallel for schedule(static)
+                for (long c = 0; c < N; ++c) reactive_cell(s, D->U1, N, c, dt);
+                if (s->err) { *t_out = t; return s->err; }
+            }
             int perr = 0;
             if (s->p.plastic) {
 #pragma omp parallel for schedule(static)
@@ -1351,13 +1518,14 @@ int tjp_run(tjp_sim* s, double final_t, int max_steps, double* dts, double* t_ou
                     c2p(s, D->U1, N, c);
                 }
             }
-            if (perr) { *t_out = t; return perr; }
+            if (perr || s->err) { *t_out = t; return perr ? perr : s->err; }
             if (s->p.radial) { /* geometricSourceTerm (radial.cpp:37-54, main.cpp:159-161) */
 #pragma omp parallel for schedule(static)
                 for (long c = 0; c < N; ++c) {
                     radial_cell(s, D, D->U1, N, c, dt);
                     c2p(s, D->U1, N, c);
                 }
+                if (s->err) { *t_out = t; return s->err; }
             }
             if (s->p.solid) {
 #pragma omp parallel for schedule(static)

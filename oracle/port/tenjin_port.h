@@ -27,10 +27,12 @@ typedef struct {
     int lo_bc[3], hi_bc[3]; /* 0 transmissive, 1 reflective */
     double cfl, thinc_beta;
     int phase[TJP_MAX_MAT]; /* 0 solid, 1 fluid */
-    int eos[TJP_MAX_MAT];   /* 0 MieGruneisen, 1 Romenskii, 2 Wilkins, 3 Hugoniot */
+    int eos[TJP_MAX_MAT];   /* 0 MieGruneisen, 1 Romenskii, 2 Wilkins, 3 Hugoniot, 4 MixtureEOS */
     double eos_params[TJP_MAX_MAT][TJP_MAX_PARAMS];
     double yield_stress[TJP_MAX_MAT];
     int radial; /* RADIAL: geometric source term (radial.cpp) after plasticUpdate */
+    int nmix;     /* numberOfMixtures: 0, or 1 with material 0 the MixtureEOS (eos 4) */
+    int reactive; /* REACTIVE: reactiveUpdate (reactive.cpp) after advance */
 } tjp_params;
 
 typedef struct tjp_sim tjp_sim;
@@ -44,8 +46,9 @@ tjp_sim* tjp_create(const tjp_params* p, int ndomains, const int* n_cells /* 3 p
 void tjp_destroy(tjp_sim* s);
 
 /* Set the initial primitive state of a domain (alpha[M], rho_k[M], u[3], p,
- * V[9] if solid, epsilon[M] if plastic; each a block over valid cells) and
- * run primitiveToConservative (initialise.cpp:111-123). */
+ * V[9] if solid, epsilon[M] if plastic, lambda if nmix; each a block over
+ * valid cells) and run primitiveToConservative (initialise.cpp:111-123); the
+ * mixture densities start at rho_k (initialise.cpp:66-71). */
 int tjp_set_primitive(tjp_sim* s, int domain, const double* prim);
 
 /* Copy a domain's full state (Ncomp blocks) in / out. */
@@ -55,7 +58,8 @@ int tjp_set_state(tjp_sim* s, int domain, const double* in);
 /* Run the time loop of main.cpp:121-191 until t >= final_t or max_steps.
  * Writes each step's dt into dts (capacity max_steps). Returns the number of
  * steps taken, or a negative error code (-1 NaN in the state, -2 NaN wave
- * speed, -3 volume-fraction scaling error, -4 plastic divide by zero). */
+ * speed, -3 volume-fraction scaling error, -4 plastic divide by zero, -5 no
+ * sign change for the mixture root bisection). */
 int tjp_run(tjp_sim* s, double final_t, int max_steps, double* dts, double* t_out);
 
 /* Number of OpenMP threads the port uses (1 when built without OpenMP). */

@@ -165,7 +165,20 @@ int main(int argc, char** argv)
         D.prim.assign(nprim, std::vector<double>(nc));
         for (int q = 0; q < nprim; ++q) rd.arr(D.prim[q].data(), nc);
     }
-    const int RADIAL = rd.i32_or(0);  // trailer: RADIAL flag
+    // trailer: RADIAL, REACTIVE, numberOfMixtures, the mixture flag of each
+    // material, then the initial lambda of each domain (absent: all zero)
+    const int RADIAL = rd.i32_or(0);
+    const int REACTIVE = rd.i32_or(0);
+    const int NMIX = rd.i32_or(0);
+    std::vector<int> mixflag(M, 0);
+    for (int m = 0; m < M; ++m) mixflag[m] = rd.i32_or(0);
+    for (auto& D : doms) {
+        long nc = (long)D.n_cells[0] * D.n_cells[1] * D.n_cells[2];
+        for (int q = 0; q < NMIX; ++q) {
+            D.prim.emplace_back(nc);
+            rd.arr(D.prim.back().data(), nc);
+        }
+    }
 
     PlasticEOS plastic;
     plastic.yieldStress.assign(M, 0.0);
@@ -178,6 +191,7 @@ int main(int argc, char** argv)
             case 1: eos[m] = new RomenskiiSolidEOS(); break;
             case 2: eos[m] = new WilkinsSolidEOS(); break;
             case 3: eos[m] = new HugoniotSolidEOS(); break;
+            case 4: eos[m] = new MixtureEOS(); break;
             default: std::fprintf(stderr, "bad eos\n"); return 2;
         }
         eos[m]->define(eosparams[m]);
@@ -188,14 +202,15 @@ int main(int argc, char** argv)
         Sim& S = sims[di];
         Domain& D = doms[di];
         ParameterStruct& Prm = S.parameters;
-        Prm.SOLID = SOLID; Prm.THINC = THINC; Prm.RADIAL = RADIAL; Prm.PLASTIC = PLASTIC; Prm.REACTIVE = 0; Prm.MUSCL = MUSCL;
-        Prm.numberOfMaterials = M; Prm.numberOfMixtures = 0; Prm.Nghost = nghost; Prm.CFL = CFL; Prm.THINCbeta = beta;
+        Prm.SOLID = SOLID; Prm.THINC = THINC; Prm.RADIAL = RADIAL; Prm.PLASTIC = PLASTIC; Prm.REACTIVE = REACTIVE; Prm.MUSCL = MUSCL;
+        Prm.numberOfMaterials = M; Prm.numberOfMixtures = NMIX; Prm.Nghost = nghost; Prm.CFL = CFL; Prm.THINCbeta = beta;
         Prm.max_grid_size = 0; Prm.dt = 0.0; Prm.x0 = 0.0;
         for (int d = 0; d < AMREX_SPACEDIM; ++d) { Prm.n_cells[d] = D.n_cells[d]; Prm.dimL[d] = D.dimL[d]; }
         Prm.materialInfo.resize(M);
         for (int m = 0; m < M; ++m) {
             Prm.materialInfo[m].phase = phase[m] == 0 ? solid : fluid;
-            Prm.materialInfo[m].mixture = 0;
+            Prm.materialInfo[m].mixture = mixflag[m];
+            Prm.materialInfo[m].mixtureIndex = 0;  // getMaterialParameters (initialise.cpp:187)
             Prm.materialInfo[m].plastic = (PLASTIC && phase[m] == 0);
             Prm.materialInfo[m].EOS = eos[m];
         }
@@ -248,6 +263,12 @@ int main(int argc, char** argv)
                                 for (int cc = 0; cc < 3; ++cc) U(i, j, k, V_TENSOR, 0, r, cc) = D.prim[q++][c];
                         if (PLASTIC)
                             for (int m = 0; m < M; ++m) U(i, j, k, EPSILON, m) = D.prim[q++][c];
+                        for (int m = 0; m < M; ++m)  // initialise.cpp:66-71
+                            if (mixflag[m]) {
+                                U(i, j, k, RHO_MIX, m, 0) = U(i, j, k, RHO_K, m);
+                                U(i, j, k, RHO_MIX, m, 1) = U(i, j, k, RHO_K, m);
+                                U(i, j, k, LAMBDA, m) = D.prim[q++][c];
+                            }
                     }
             U.primitiveToConservative();
         }
@@ -276,6 +297,7 @@ int main(int argc, char** argv)
             *S.U = *S.U1;
             advance(*S.U, *S.U1, *S.U2, *S.UL, *S.UR, *S.MUSCLgrad, *S.ULStar, *S.URStar, *S.UStarStar, S.flux_arr,
                     S.geom, Prm, S.bc, *S.THINCArr);
+            if (Prm.REACTIVE) reactiveUpdate(*S.U, *S.U1, *S.U2, Prm);
             if (Prm.PLASTIC) plastic.plasticUpdate(*S.U1, Prm);
             if (Prm.RADIAL) geometricSourceTerm(*S.U1, Prm);
             if (Prm.SOLID) S.U1->cleanUpV();

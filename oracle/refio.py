@@ -51,8 +51,14 @@ def write_input(case, path: str) -> None:
             for b in d.boxes:
                 w(struct.pack("<6i", *b))
             assert d.prim.shape[0] == case.nprim
-            w(np.ascontiguousarray(d.prim, dtype="<f8").tobytes())
-        w(struct.pack("<i", int(getattr(case, "radial", 0))))
+            nmix = case.nmix
+            w(np.ascontiguousarray(d.prim[:case.nprim - nmix], dtype="<f8").tobytes())
+        # trailer: RADIAL, REACTIVE, numberOfMixtures, mixture flags, lambda rows
+        w(struct.pack("<3i", int(case.radial), int(case.reactive), case.nmix))
+        w(struct.pack(f"<{case.M}i", *[int(m.eos == 4) for m in case.materials]))
+        for d in case.domains:
+            if case.nmix:
+                w(np.ascontiguousarray(d.prim[case.nprim - case.nmix:], dtype="<f8").tobytes())
 
 
 def read_output(case, path: str):

@@ -33,6 +33,7 @@ EOS_MIEGRUNEISEN = 0
 EOS_ROMENSKII = 1
 EOS_WILKINS = 2
 EOS_HUGONIOT = 3
+EOS_MIXTURE = 4   # two stiffened gases blended by the mass fraction lambda
 
 PHASE_SOLID = 0
 PHASE_FLUID = 1
@@ -71,6 +72,7 @@ class Case:
     plastic: int = 0
     muscl: int = 1
     radial: int = 0               # RADIAL: geometric source term, x the radius
+    reactive: int = 0             # REACTIVE: reactiveUpdate of the mixture's mass fraction
     nghost: int = 2
     lo_bc: List[int] = dataclasses.field(default_factory=lambda: [0, 0, 0])
     hi_bc: List[int] = dataclasses.field(default_factory=lambda: [0, 0, 0])
@@ -85,8 +87,15 @@ class Case:
         return len(self.materials)
 
     @property
+    def nmix(self) -> int:
+        """numberOfMixtures: the materials with the MixtureEOS (material 0 only)."""
+        return sum(1 for m in self.materials if m.eos == EOS_MIXTURE)
+
+    @property
     def nprim(self) -> int:
-        return 2 * self.M + 4 + (9 if self.solid else 0) + (self.M if self.plastic else 0)
+        """Primitive input rows: alpha[M], rho_k[M], u[3], p, V[9] (solid),
+        epsilon[M] (plastic), lambda (mixture)."""
+        return 2 * self.M + 4 + (9 if self.solid else 0) + (self.M if self.plastic else 0) + self.nmix
 
     @property
     def total_cells(self) -> int:
@@ -234,6 +243,64 @@ def shock_bubble_2d(n: int = 1024, seed: int = 0, max_grid_size: int = 128, max_
         prim[4, 0] += 10.0 * background * smooth_field(rng, n)
         prim[5, 0] += 10.0 * background * smooth_field(rng, n)
     c.domains = [Domain(nn, [1.0, 1.0, 1.0], max_size_boxes(nn, 2, max_grid_size), prim)]
+    return c
+
+
+# ---------------------------------------------------------------------------
+# Parity workload for the MixtureEOS and the reactive update: a condensed
+# explosive (reactant/products mixture, material 0) next to air.
+# ---------------------------------------------------------------------------
+
+EXPL_REACTANT = [2.5, -2.5 * 1.0e7, 4.0e6, 1500.0]   # [gamma, pref, eref, CV]: stiffened, p_inf 1e7
+EXPL_PRODUCTS = [1.4, 0.0, 0.0, 1000.0]
+EXPL_RHO = 1600.0
+
+
+def reactive_charge(dim: int = 1, n: int = 200, length: float = 0.1, max_grid_size: int = 64,
+                    max_steps: int = 60, reactive: int = 1, thinc: int = 0, seed: int = 0,
+                    eps: float = 1e-6, products: Optional[List[float]] = None, reactant: Optional[List[float]] = None,
+                    ambient_p: float = 1.0e8, air_rho: float = 100.0) -> Case:
+    """Explosive (MixtureEOS: reactant and products, lambda = reactant mass
+    fraction) filling x < length/2 in 1-D (a disc of radius 0.3 length about the
+    centre in 2-D), compressed air elsewhere, all at ambient_p (the
+    pressure-based rate raises p to the power 1.2, reactive.cpp:19, so
+    p must stay positive); a hot spot at 2 GPa (x < length/10, or a
+    disc of radius 0.08 length) starts the pressure-based burn of
+    reactive.cpp:3-26 when `reactive`. Lambda is 1 - 5e-4 except for a
+    seeded partly-burnt patch (lambda in (0.2, 0.9)) that sends the closure
+    through the bisection of equationofstate.cpp:274-376 from the first step."""
+    mats = [Material(PHASE_FLUID, EOS_MIXTURE, list(reactant or EXPL_REACTANT) + list(products or EXPL_PRODUCTS)),
+            Material(PHASE_FLUID, EOS_MIEGRUNEISEN, _stiffened(AIR_GAMMA, 0.0))]
+    c = Case(f"reactive_charge_{dim}d", dim, mats, thinc=thinc, reactive=reactive, cfl=0.4, max_steps=max_steps)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    nn = [n, n if dim > 1 else 1, 1]
+    prim = _empty_prim(c, nn)
+    xc = (np.arange(n) + 0.5) / n
+    if dim == 1:
+        X = xc[None, :]
+        charge = X < 0.5
+        hot = X < 0.1
+        patch = (X > 0.2) & (X < 0.3)
+    else:
+        X, Y = np.meshgrid(xc, xc, indexing="xy")
+        r2 = (X - 0.5) ** 2 + (Y - 0.5) ** 2
+        charge = r2 < 0.09
+        hot = r2 < 0.0064
+        patch = (np.abs(X - 0.5) < 0.1) & (Y > 0.62) & (Y < 0.72)
+    a0 = np.where(charge, 1.0 - eps, eps)
+    prim[0, 0] = a0
+    prim[1, 0] = 1.0 - a0
+    prim[2, 0] = EXPL_RHO
+    prim[3, 0] = air_rho
+    prim[7, 0] = np.where(hot, 2.0e9, ambient_p)
+    # unburnt lambda = 1 - 5e-4: at lambda = 1 exactly defineMixtureDensities
+    # (equationofstate.cpp:390-396) gives rhomix_1 = 0/0 and the energy of the
+    # reconstructed states NaN
+    lam = np.full(a0.shape, 1.0 - 5e-4)
+    lam[patch] = rng.uniform(0.2, 0.9, size=int(patch.sum()))
+    prim[c.nprim - 1, 0] = lam
+    L = [length, length if dim > 1 else 1.0, 1.0]
+    c.domains = [Domain(nn, L, max_size_boxes(nn, dim, max_grid_size), prim)]
     return c
 
 

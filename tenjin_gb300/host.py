@@ -188,15 +188,20 @@ def carried_components(case: Case):
     """AccessPattern indices of the components that carry state from one step
     to the next (the rest -- sound speed, stress, Hencky strain, USTAR/VSTAR --
     are recomputed before use). HJ2 is carried for solids: the CFL sound speed
-    of the solid EOS reads it."""
+    of the solid EOS reads it; the mixture densities are carried for the
+    MixtureEOS: the RK2 average leaves them in the state the CFL sound speed
+    reads (equationofstate.cpp:208-220)."""
     M = case.M
     idx = list(range(0, 3 * M + 1))            # alpha, alphaRho, rho_k, rho
     base = 3 * M + 1
     idx += list(range(base, base + 3))         # rhoU
     idx += list(range(base + 3, base + 6))     # u
     idx += [base + 6, base + 7]                # E, p
+    nmix = getattr(case, "nmix", 0)
+    x0 = base + 8 + 1 + 1 + 9                  # after a, uStar, sigma
+    idx += list(range(x0, x0 + 4 * nmix))      # rhomix (2), lambda, alphaRhoLambda
     if case.solid:
-        v0 = base + 8 + 1 + 1 + 9              # after a, uStar, sigma
+        v0 = x0 + 4 * nmix
         idx += list(range(v0, v0 + 9))         # V
         idx += [v0 + 27]                       # HenckyJ2
         if case.plastic:

@@ -53,6 +53,10 @@ def variable_names(case: Case) -> List[str]:
     add("a")
     add("uStar")
     add("sigma", 1, 3, 3)
+    nmix = getattr(case, "nmix", 0)
+    add("rhomix", nmix, 2)
+    add("lambda", nmix)
+    add("alpharholambda", nmix)
     if case.solid:
         add("V", 1, 3, 3)
         add("VStar", 1, 3, 3)

@@ -45,6 +45,14 @@ FIXTURES = {
                            {"radial": 1, "lo_bc": [1, 1, 0], "hi_bc": [1, 0, 0]}),
     "wilkins2d_plastic_cylindrical": ("solid_mixture_2d", {"eos": cases.EOS_WILKINS, "n": 20, "max_steps": 10},
                                       {"radial": 1, "lo_bc": [1, 0, 0]}),
+    # MixtureEOS (reactant/products, bisection closure) and the reactive update
+    "reactive_charge_1d": ("reactive_charge", {"dim": 1, "n": 200, "max_steps": 120}),
+    "reactive_charge_2d_thinc": ("reactive_charge", {"dim": 2, "n": 48, "max_grid_size": 16, "max_steps": 40,
+                                                     "thinc": 1}),
+    "mixture_closed_form_2d": ("reactive_charge", {"dim": 2, "n": 40, "max_grid_size": 16, "max_steps": 30,
+                                                   "reactive": 0, "reactant": [2.5, 0.0, 4.0e6, 1500.0]}),
+    "reactive_spherical_1d": ("reactive_charge", {"dim": 1, "n": 160, "max_grid_size": 40, "max_steps": 100},
+                              {"radial": 1, "lo_bc": [1, 0, 0]}),
 }
 
 
