@@ -39,6 +39,7 @@ extern "C" {
 #define TJ_ERR_ALPHA -5      /* volume-fraction scaling error (boxaccesscellarray.cpp:553-588) */
 #define TJ_ERR_PLASTIC -6    /* plastic divide by zero (plastic.cpp:189-193) */
 #define TJ_ERR_STATE -7      /* call out of order (no domain, no state) */
+#define TJ_ERR_ROOT -8       /* no sign change in the mixture root bisection (equationofstate.cpp:327-335) */
 
 /* equation-of-state kinds; parameter vectors as getMaterialParameters builds
  * them (initialise.cpp:125-235) */
@@ -47,6 +48,9 @@ extern "C" {
 #define TJ_EOS_WILKINS 2      /* [gamma, pref, eref, CV, rho0, e1..e5, G0]       equationofstate.cpp:502-596 */
 #define TJ_EOS_HUGONIOT 3     /* [gamma, pref, eref, CV, rho0, c0, s, G0]: linear us-up Hugoniot reference
                                  curve with constant Gruneisen gamma; no reference counterpart */
+#define TJ_EOS_MIXTURE 4      /* [gamma, pref, eref, CV] of the reactant, then of the products:
+                                 MixtureEOS (equationofstate.cpp:117-396), a "mixture" fluid; material
+                                 0 only, with n_mixtures = 1 */
 
 #define TJ_PHASE_SOLID 0 /* Material_type (structdefinitions.h:36-40) */
 #define TJ_PHASE_FLUID 1
@@ -74,9 +78,9 @@ typedef struct tj_material {
 typedef struct tj_params {
     int dim;          /* AMREX_SPACEDIM: 1, 2 or 3 */
     int n_materials;  /* numberOfMaterials */
-    int n_mixtures;   /* numberOfMixtures: must be 0 */
-    int SOLID, THINC, RADIAL, PLASTIC, REACTIVE, MUSCL; /* REACTIVE: must be 0; RADIAL: not with
-                                                          elastic solids (SOLID without PLASTIC) */
+    int n_mixtures;   /* numberOfMixtures: 0, or 1 with material 0 a TJ_EOS_MIXTURE fluid */
+    int SOLID, THINC, RADIAL, PLASTIC, REACTIVE, MUSCL; /* RADIAL: not with elastic solids (SOLID
+                                                          without PLASTIC); mixtures: SOLID = 0 */
     int nghost;       /* Nghost: must be >= 2 */
     int lo_bc[3], hi_bc[3];
     double CFL, THINCbeta;
@@ -119,9 +123,10 @@ int tj_download_state(tj_ctx* ctx, int domain, int box, double* fab, int ncomp, 
 int tj_upload_domain(tj_ctx* ctx, int domain, const double* data);
 int tj_download_domain(tj_ctx* ctx, int domain, double* data);
 /* Initial condition from primitive fields (alpha[M], rho_k[M], u[3], p,
- * V[9] if SOLID, epsilon[M] if PLASTIC; each nx*ny*nz doubles), then
- * primitiveToConservative: the last step of setInitialConditions
- * (initialise.cpp:111-123). */
+ * V[9] if SOLID, epsilon[M] if PLASTIC, lambda if n_mixtures; each nx*ny*nz
+ * doubles), then primitiveToConservative: the last step of
+ * setInitialConditions (initialise.cpp:111-123). The mixture densities start
+ * at rho_k (initialise.cpp:66-71). */
 int tj_set_primitive(tj_ctx* ctx, int domain, const double* prim);
 
 /* Operators of the time loop. */
@@ -138,6 +143,11 @@ int tj_plastic_update(tj_ctx* ctx, double dt);
  * conservativeToPrimitive left it. tj_step applies it after plasticUpdate
  * when RADIAL is set (main.cpp:159-161). */
 int tj_geometric_source(tj_ctx* ctx, double dt);
+/* reactiveUpdate (reactive.cpp:60-103): the pressure-based burn of the
+ * mixture's mass fraction by two Euler steps averaged with the start value,
+ * then conservativeToPrimitive. A no-op without mixtures. tj_step applies it
+ * after advance when REACTIVE is set (main.cpp:149-152). */
+int tj_reactive_update(tj_ctx* ctx, double dt);
 /* CellArray::cleanUpV (boxaccesscellarray.cpp:476-528). */
 int tj_cleanup_v(tj_ctx* ctx);
 /* CellArray::cleanUpAlpha (boxaccesscellarray.cpp:530-599). */
@@ -151,8 +161,8 @@ int tj_contains_nan(tj_ctx* ctx, int* flag);
 
 /* One iteration of the time loop of main.cpp:121-191 with dt and t kept on
  * the device: dt = getTimeStep, clamped to t_end, times 0.2 for the first
- * five steps; advance; plasticUpdate (PLASTIC); geometricSourceTerm (RADIAL);
- * cleanUpV (SOLID);
+ * five steps; advance; reactiveUpdate (REACTIVE); plasticUpdate (PLASTIC);
+ * geometricSourceTerm (RADIAL); cleanUpV (SOLID);
  * cleanUpAlpha; NaN check. Does not synchronise. */
 int tj_step(tj_ctx* ctx, double t_end);
 /* Run up to nsteps iterations or until t >= t_end. Steps are issued in

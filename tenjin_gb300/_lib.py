@@ -16,7 +16,7 @@ TJ_MAX_EOS_PARAMS = 16
 TJ_OK = 0
 ERRORS = {
     -1: "TJ_ERR_ARG", -2: "TJ_ERR_CUDA", -3: "TJ_ERR_NAN", -4: "TJ_ERR_WAVESPEED",
-    -5: "TJ_ERR_ALPHA", -6: "TJ_ERR_PLASTIC", -7: "TJ_ERR_STATE",
+    -5: "TJ_ERR_ALPHA", -6: "TJ_ERR_PLASTIC", -7: "TJ_ERR_STATE", -8: "TJ_ERR_ROOT",
 }
 TJ_PRECISION_FP64 = 0
 TJ_PRECISION_MIXED = 1
@@ -63,6 +63,7 @@ SIGNATURES = [
     ("tj_compute_dt", _I, [_P, _PD]),
     ("tj_advance", _I, [_P, _D]),
     ("tj_plastic_update", _I, [_P, _D]),
+    ("tj_reactive_update", _I, [_P, _D]),
     ("tj_geometric_source", _I, [_P, _D]),
     ("tj_cleanup_v", _I, [_P]),
     ("tj_cleanup_alpha", _I, [_P]),

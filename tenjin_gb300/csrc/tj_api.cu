@@ -152,6 +152,8 @@ void make_layouts(const tj_params& p, DevParams& P)
     P.muscl = p.MUSCL;
     P.fused64 = p.precision == TJ_PRECISION_FUSED64;
     P.radial = p.RADIAL ? 1 : 0;
+    P.nmix = p.n_mixtures;
+    P.reactive = p.REACTIVE ? 1 : 0;
     P.S_ELO = -1;
     for (int d = 0; d < 3; ++d) { P.lo_bc[d] = p.lo_bc[d]; P.hi_bc[d] = p.hi_bc[d]; }
     P.cfl = p.CFL;
@@ -175,6 +177,8 @@ void make_layouts(const tj_params& p, DevParams& P)
     P.S_V = P.S_HJ2 = P.S_EPS = P.S_ARE = -1;
     if (P.solid) { P.S_V = n; n += 9; P.S_HJ2 = n++; }
     if (P.plastic) { P.S_EPS = n; n += M; P.S_ARE = n; n += M; }
+    P.S_RMIX = P.S_LAM = P.S_ARL = -1;
+    if (P.nmix) { P.S_RMIX = n; n += 2; P.S_LAM = n++; P.S_ARL = n++; }
     P.NS = n;
     n = 0;
     P.F_ALPHA = n; n += M;
@@ -188,6 +192,7 @@ void make_layouts(const tj_params& p, DevParams& P)
     P.F_SIGMA = P.F_V = P.F_ARE = -1;
     if (P.solid) { P.F_SIGMA = n; n += 9; P.F_V = n; n += 9; }
     if (P.plastic) { P.F_ARE = n; n += M; }
+    P.F_ARL = P.nmix ? n++ : -1;
     P.NF = n;
     n = 0;
     P.X_ALPHA = n; n += M;
@@ -197,11 +202,12 @@ void make_layouts(const tj_params& p, DevParams& P)
     P.X_V = P.X_ARE = -1;
     if (P.solid) { P.X_V = n; n += 9; }
     if (P.plastic) { P.X_ARE = n; n += M; }
+    P.X_ARL = P.nmix ? n++ : -1;
     P.X_SSTAR = n++;
     P.X_VSTAR = -1;
     if (P.solid) { P.X_VSTAR = n; n += 3; }
     P.NX = n;
-    // AccessPattern (accesspattern.cpp:44-79), no mixtures
+    // AccessPattern (accesspattern.cpp:44-79)
     n = 0;
     P.A_ALPHA = n; n += M;
     P.A_ARHO = n; n += M;
@@ -214,6 +220,8 @@ void make_layouts(const tj_params& p, DevParams& P)
     P.A_A = n++;
     P.A_USTAR = n++;
     P.A_SIGMA = n; n += 9;
+    P.A_RMIX = P.A_LAM = P.A_ARL = -1;
+    if (P.nmix) { P.A_RMIX = n; n += 2; P.A_LAM = n++; P.A_ARL = n++; }
     P.A_V = P.A_VSTAR = P.A_DEVH = P.A_HJ2 = P.A_EPS = P.A_ARE = -1;
     if (P.solid) {
         P.A_V = n; n += 9;
@@ -368,6 +376,8 @@ int check_status(tj_ctx* c)
                            : s.status == TJ_ERR_ALPHA   ? "error in scaling volume fractions (boxaccesscellarray.cpp:553-588)"
                            : s.status == TJ_ERR_PLASTIC ? "divide by zero in the plastic update (plastic.cpp:189-193)"
                            : s.status == TJ_ERR_NAN     ? "NaN found in the state (main.cpp:183-187)"
+                           : s.status == TJ_ERR_ROOT    ? "no sign change in the mixture root bisection "
+                                                          "(equationofstate.cpp:327-335)"
                                                         : "device error";
         return fail(c, s.status, what);
     }
@@ -410,8 +420,19 @@ int tj_create(const tj_params* p, tj_ctx** out)
     };
     if (p->dim < 1 || p->dim > 3) return bad("dim must be 1, 2 or 3");
     if (p->n_materials < 1 || p->n_materials > TJ_MAX_MATERIALS) return bad("n_materials out of range");
-    if (p->n_mixtures != 0) return bad("mixtures (MixtureEOS) are not supported");
-    if (p->REACTIVE) return bad("REACTIVE is not supported");
+    if (p->n_mixtures < 0 || p->n_mixtures > 1)
+        return bad("n_mixtures must be 0 or 1: the reference indexes every mixture at mixtureIndex 0 "
+                   "(initialise.cpp:187, boxaccesscellarray.cpp:43-47)");
+    {
+        int nmixeos = 0;
+        for (int m = 0; m < p->n_materials && m < TJ_MAX_MATERIALS; ++m) nmixeos += p->materials[m].eos == TJ_EOS_MIXTURE;
+        if (nmixeos != p->n_mixtures) return bad("n_mixtures must equal the number of TJ_EOS_MIXTURE materials");
+        if (p->n_mixtures && p->materials[0].eos != TJ_EOS_MIXTURE)
+            return bad("the mixture must be material 0 (the reference's Cell maps mixture 0 to material 0, "
+                       "cell.cpp:95-97, hllc.cpp:26-29)");
+        if (p->n_mixtures && p->materials[0].phase != TJ_PHASE_FLUID) return bad("a mixture is a fluid (initialise.cpp:158-178)");
+        if (p->n_mixtures && p->SOLID) return bad("mixtures with SOLID are not supported");
+    }
     if (p->RADIAL && p->SOLID && !p->PLASTIC)
         return bad("RADIAL with elastic solids is not supported: the source term reads the RK2-averaged stress "
                    "(hllc.cpp:705, radial.cpp:23), which the carried state does not hold");
@@ -424,12 +445,12 @@ int tj_create(const tj_params* p, tj_ctx** out)
     int any_solid = 0;
     for (int m = 0; m < p->n_materials; ++m) {
         const tj_material& mt = p->materials[m];
-        if (mt.eos < 0 || mt.eos > TJ_EOS_HUGONIOT) return bad("unknown EOS");
+        if (mt.eos < 0 || mt.eos > TJ_EOS_MIXTURE) return bad("unknown EOS");
         int need = mt.eos == TJ_EOS_MIEGRUNEISEN ? 4 : mt.eos == TJ_EOS_ROMENSKII ? 9 : mt.eos == TJ_EOS_WILKINS ? 11 : 8;
         if (mt.nparams < need) return bad("too few EOS parameters");
         if (mt.phase == TJ_PHASE_SOLID) {
             any_solid = 1;
-            if (mt.eos == TJ_EOS_MIEGRUNEISEN) return bad("a solid needs a solid EOS");
+            if (mt.eos == TJ_EOS_MIEGRUNEISEN || mt.eos == TJ_EOS_MIXTURE) return bad("a solid needs a solid EOS");
         }
     }
     if (p->SOLID && !any_solid) return bad("SOLID needs a solid material");
@@ -660,7 +681,7 @@ int tj_set_primitive(tj_ctx* c, int q, const double* prim)
     int e = need_state(c);
     if (e) return e;
     const DevDomain& D = c->doms[q];
-    int nprim = 2 * c->P.M + 4 + (c->P.solid ? 9 : 0) + (c->P.plastic ? c->P.M : 0);
+    int nprim = 2 * c->P.M + 4 + (c->P.solid ? 9 : 0) + (c->P.plastic ? c->P.M : 0) + c->P.nmix;
     size_t bytes = sizeof(double) * nprim * (size_t)D.n[0] * D.n[1] * D.n[2];
     e = ensure_staging(c, bytes);
     if (e) return e;
@@ -732,6 +753,14 @@ int tj_plastic_update(tj_ctx* c, double dt)
     if (!c->P.plastic) return TJ_OK;
     return cell_op(c, OP_PLASTIC);
 }
+int tj_reactive_update(tj_ctx* c, double dt)
+{
+    if (!c) return TJ_ERR_ARG;
+    if (!(dt >= 0.0)) return fail(c, TJ_ERR_ARG, "tj_reactive_update: dt must be >= 0");
+    if (!c->P.nmix) return TJ_OK;  // reactive.cpp:64
+    return cell_op(c, OP_REACTIVE, dt);
+}
+
 int tj_geometric_source(tj_ctx* c, double dt)
 {
     if (!c) return TJ_ERR_ARG;

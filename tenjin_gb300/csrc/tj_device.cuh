@@ -26,12 +26,14 @@ struct CellT {
     R V[9], devH[9], hj2;
     R eps[TJ_MAX_MAT], are[TJ_MAX_MAT];
     R Elo;  // binary32 state: the low word of the compensated total energy
+    R lam, arl, rm0, rm1;  // MixtureEOS (material 0): lambda, alphaRhoLambda, rhomix rows 0 and 1
 };
 using CellS = CellT<double>;
 
 template <typename R>
 struct ECellT {
     R alpha, arho, rhok, p, hj2;
+    R lam, rm0, rm1;  // MixtureEOS only
 };
 using ECell = ECellT<double>;
 
@@ -44,6 +46,9 @@ __device__ __forceinline__ ECellT<R> ecell_of(const CellT<R>& c, int m)
     e.rhok = c.rhok[m];
     e.p = c.p;
     e.hj2 = c.hj2;
+    e.lam = c.lam;
+    e.rm0 = c.rm0;
+    e.rm1 = c.rm1;
     return e;
 }
 
@@ -58,6 +63,17 @@ __device__ __forceinline__ typename PT::real gam(const PT& P, int m)
     return P.prm[m][0] - R(1.0);
 }
 
+// MixtureEOS (equationofstate.cpp:117-396): two stiffened gases, parameters
+// [gamma, pref, eref, CV] x 2, blended by the mass fraction lambda. The
+// effective gamma - 1 of :175 and :224.
+template <typename PT>
+__device__ __forceinline__ typename PT::real mix_gamma_term(const PT& P, int m, typename PT::real lam)
+{
+    using R = typename PT::real;
+    const R* q = P.prm[m];
+    return (lam * q[0] * q[3] + (R(1.0) - lam) * q[4] * q[7]) / (lam * q[3] + (R(1.0) - lam) * q[7]) - R(1.0);
+}
+
 template <typename PT>
 __device__ inline typename PT::real eos_e_cold(const PT& P, int m, const ECellT<typename PT::real>& e)
 {
@@ -65,6 +81,7 @@ __device__ inline typename PT::real eos_e_cold(const PT& P, int m, const ECellT<
     const R* q = P.prm[m];
     switch (P.eos[m]) {
         case TJ_EOS_MIEGRUNEISEN: return q[2] * e.arho;  // equationofstate.cpp:37-40
+        case TJ_EOS_MIXTURE: return e.lam * (q[2] * e.arho) + (R(1.0) - e.lam) * (q[6] * e.arho);  // :161-165
         case TJ_EOS_ROMENSKII: {                         // :418-423
             R a = q[6], K0 = q[5], r0 = q[4], x = e.rhok / r0;
             return e.arho * (((K0 / (R(2.0) * r0 * a * a)) * (tjm_pow(x, a) - R(1.0))) * (tjm_pow(x, a) - R(1.0)));
@@ -90,6 +107,9 @@ __device__ inline typename PT::real eos_p_cold(const PT& P, int m, const ECellT<
     R G = gam(P, m);
     switch (P.eos[m]) {
         case TJ_EOS_MIEGRUNEISEN: return q[1] * e.alpha / G;  // :42-45
+        case TJ_EOS_MIXTURE:                                  // :167-171
+            return (q[1] * e.alpha / (q[0] - R(1.0))) * e.lam * e.rhok / (e.rm0) +
+                   (q[5] * e.alpha / (q[4] - R(1.0))) * (R(1.0) - e.lam) * e.rhok / (e.rm1);
         case TJ_EOS_ROMENSKII: {                              // :425-430
             R a = q[6], K0 = q[5], r0 = q[4], x = e.rhok / r0;
             return (e.alpha / G) * ((K0 / a) * tjm_pow(x, a + R(1.0)) * (tjm_pow(x, a) - R(1.0)));
@@ -114,6 +134,7 @@ __device__ inline typename PT::real eos_G(const PT& P, int m, const ECellT<typen
     const R* q = P.prm[m];
     switch (P.eos[m]) {
         case TJ_EOS_MIEGRUNEISEN: return R(0.0) * e.alpha;                           // :81-84
+        case TJ_EOS_MIXTURE: return R(0.0);                                          // :146-149
         case TJ_EOS_ROMENSKII: return q[8] * tjm_pow((e.rhok / q[4]), q[7] + R(1.0));  // :437-440
         case TJ_EOS_WILKINS: return q[10];                                           // :538-541
         default: return q[7];
@@ -151,6 +172,7 @@ __device__ inline typename PT::real eos_e_shear(const PT& P, int m, const ECellT
     using R = typename PT::real;
     switch (P.eos[m]) {
         case TJ_EOS_MIEGRUNEISEN: return R(0.0) * e.alpha;  // :101-104
+        case TJ_EOS_MIXTURE: return R(0.0);                 // :136-139
         case TJ_EOS_HUGONIOT: return e.alpha * (P.prm[m][7] * e.hj2);
         default: return e.alpha * (eos_G(P, m, e) * e.hj2);  // :457-460, :558-561
     }
@@ -163,6 +185,7 @@ __device__ inline typename PT::real eos_p_shear(const PT& P, int m, const ECellT
     R G = gam(P, m);
     switch (P.eos[m]) {
         case TJ_EOS_MIEGRUNEISEN: return R(0.0) * e.alpha;  // :106-109
+        case TJ_EOS_MIXTURE: return R(0.0);                 // :141-144
         case TJ_EOS_HUGONIOT: return (e.alpha / G) * ((e.rhok * R(0.0) - P.prm[m][7]) * e.hj2);
         default: return (e.alpha / G) * ((e.rhok * eos_dGdrho(P, m, e) - eos_G(P, m, e)) * e.hj2);  // :462-465
     }
@@ -171,7 +194,17 @@ __device__ inline typename PT::real eos_p_shear(const PT& P, int m, const ECellT
 template <typename PT>
 __device__ __forceinline__ typename PT::real eos_invG(const PT& P, int m, const ECellT<typename PT::real>& e)
 {
+    if (P.eos[m] == TJ_EOS_MIXTURE) return e.alpha / mix_gamma_term(P, m, e.lam);  // :173-178
     return e.alpha / gam(P, m);
+}
+
+// xi (equationofstate.cpp:72-75, 222-225)
+template <typename PT>
+__device__ __forceinline__ typename PT::real eos_xi(const PT& P, int m, const ECellT<typename PT::real>& e)
+{
+    using R = typename PT::real;
+    if (P.eos[m] == TJ_EOS_MIXTURE) return R(1.0) / mix_gamma_term(P, m, e.lam);
+    return R(1.0) / gam(P, m);
 }
 
 // Sound-speed contribution c^2_m (getSoundSpeedContribution).
@@ -183,6 +216,12 @@ __device__ inline typename PT::real eos_c2(const PT& P, int m, const ECellT<type
     R G = gam(P, m);
     switch (P.eos[m]) {
         case TJ_EOS_MIEGRUNEISEN: return e.p * (G + R(1.0)) / e.rhok - q[1] / e.rhok;  // :61-64
+        case TJ_EOS_MIXTURE: {  // mixtureSoundSpeed (:208-220)
+            const R G1 = q[0] - R(1.0), G2 = q[4] - R(1.0);
+            R dedrho = (e.lam) * ((q[1] - e.p) / (G1 * e.rhok * e.rhok));
+            dedrho += (R(1.0) - e.lam) * ((q[5] - e.p) / (G2 * e.rhok * e.rhok));
+            return (e.p / (e.rhok * e.rhok) - dedrho) / (e.lam / (e.rm0 * G1) + (R(1.0) - e.lam) / (e.rm1 * G2));
+        }
         case TJ_EOS_ROMENSKII: {                                                       // :432-435
             R a = q[6], K0 = q[5], r0 = q[4], x = e.rhok / r0;
             R dpc = (K0 / (a * r0)) * tjm_pow(x, a) * ((R(2.0) * a + R(1.0)) * tjm_pow(x, a) - (a + R(1.0)));
@@ -446,11 +485,84 @@ __device__ inline void stress(const PT& P, CellT<typename PT::real>& c)
         }
 }
 
-// conservativeToPrimitive (:67-122)
+// MixtureEOS root finding (equationofstate.cpp:238-376) for material 0, in
+// binary64: the mixture densities at which the two components' temperatures
+// (p - pref)/(rho Gamma CV) agree, by bisection of rhomix_0 on
+// [lambda rho_k + 1e-10, 1e6] to a relative width of 1e-7. Returns
+// TJ_ERR_ROOT where the reference prints and exits (no sign change over the
+// bracket), and after kMaxBisect halvings (the reference loops on; the width
+// test passes after about 60 at most).
+constexpr int kMaxBisect = 200;
+
+__device__ __forceinline__ double mix_rhob(const CellT<double>& c, double rhoa)  // rhobFunc (:243-246)
+{
+    return (1.0 - c.lam) / (1.0 / c.rhok[0] - c.lam / rhoa);
+}
+
+__device__ __forceinline__ int sgn_d(double v) { return (0.0 < v) - (v < 0.0); }
+
+template <typename PD>
+__device__ inline double mix_bisect_f(const PD& P, CellT<double>& c, double rho_try, double ke)  // :262-272
+{
+    c.rm0 = rho_try;
+    c.rm1 = mix_rhob(c, rho_try);
+    const double p = (c.E - ke - eff_e_nonthermal(P, c) + eff_p_nonthermal(P, c)) / (eff_invG(P, c));
+    const double* q = P.prm[0];
+    // pressureFunction (:251-260)
+    return ((p - q[1]) / (c.rm0 * (q[0] - 1.0) * q[3])) - ((p - q[5]) / (c.rm1 * (q[4] - 1.0) * q[7]));
+}
+
+template <typename PD>
+__device__ inline int mix_root_find(const PD& P, CellT<double>& c, double ke)
+{
+    const double* q = P.prm[0];
+    const double lam = c.lam, rk = c.rhok[0];
+    if (q[1] == 0.0 && q[5] == 0.0) {
+        c.rm0 = rk * (lam + (1.0 - lam) * ((q[4] - 1.0) * q[7]) / ((q[0] - 1.0) * q[3]));
+        c.rm1 = mix_rhob(c, c.rm0);
+        return 0;
+    }
+    if (lam > 1.0 - 1E-3) {
+        c.rm0 = rk;
+        c.rm1 = rk;
+        return 0;
+    } else if (lam < 1E-3) {
+        c.rm1 = rk;
+        c.rm0 = rk;
+        return 0;
+    }
+    double A = lam * rk + 1E-10, B = 1000000.0;
+    double mid = 0.5 * (A + B);
+    if (fabs(mix_bisect_f(P, c, A, ke)) <= 1E-4) {
+        c.rm0 = A;
+        c.rm1 = mix_rhob(c, c.rm0);
+        return 0;
+    } else if (fabs(mix_bisect_f(P, c, B, ke)) <= 1E-4) {
+        c.rm0 = B;
+        c.rm1 = mix_rhob(c, c.rm0);
+        return 0;
+    }
+    if (sgn_d(mix_bisect_f(P, c, A, ke)) == sgn_d(mix_bisect_f(P, c, B, ke))) return TJ_ERR_ROOT;
+    for (int n = 0; n < kMaxBisect; ++n) {
+        if (sgn_d(mix_bisect_f(P, c, mid, ke)) == sgn_d(mix_bisect_f(P, c, A, ke))) A = mid;
+        else B = mid;
+        mid = 0.5 * (A + B);
+        if (fabs(A - B) / (A + B) < 1E-7) {
+            c.rm0 = mid;
+            c.rm1 = mix_rhob(c, c.rm0);
+            return 0;
+        }
+    }
+    return TJ_ERR_ROOT;
+}
+
+// conservativeToPrimitive (:67-122). Returns 0, or TJ_ERR_ROOT from the
+// mixture closure.
 template <typename PT>
-__device__ inline void c2p(const PT& P, CellT<typename PT::real>& c)
+__device__ inline int c2p(const PT& P, CellT<typename PT::real>& c)
 {
     using R = typename PT::real;
+    int err = 0;
     c.rho = 0;
     for (int m = 0; m < P.M; ++m) {
         c.rhok[m] = c.arho[m] / c.alpha[m];
@@ -465,14 +577,37 @@ __device__ inline void c2p(const PT& P, CellT<typename PT::real>& c)
         ke += R(0.5) * c.rho * c.vel[r] * c.vel[r];
     }
     if constexpr (sizeof(R) == 4) {
-        // binary32 state: the closure of the pressure in binary64, from the
-        // compensated energy (E, Elo) and binary64 cold terms
+        // binary32 state: the closure of the pressure (and of the mixture
+        // densities) in binary64, from the compensated energy (E, Elo) and
+        // binary64 cold terms
         double rho = 0.0, ked = 0.0, ent = 0.0, pnt = 0.0, ig = 0.0;
         for (int m = 0; m < P.M; ++m) rho += (double)c.arho[m];
 #pragma unroll
         for (int r = 0; r < 3; ++r) {
             const double u = (double)c.rhou[r] / rho;
             ked += 0.5 * rho * u * u;
+        }
+        double lam = 0.0, rm0 = 0.0, rm1 = 0.0;
+        if (P.nmix) {
+            lam = (double)c.arl / (double)c.arho[0];
+            CellT<double> cd;
+            for (int m = 0; m < P.M; ++m) {
+                cd.alpha[m] = c.alpha[m];
+                cd.arho[m] = c.arho[m];
+                cd.rhok[m] = c.rhok[m];
+            }
+            cd.hj2 = c.hj2;
+            cd.p = 0.0;
+            cd.E = (double)c.E + (double)c.Elo;
+            cd.lam = lam;
+            cd.rm0 = c.rm0;
+            cd.rm1 = c.rm1;
+            err = mix_root_find(P.d, cd, ked);
+            rm0 = cd.rm0;
+            rm1 = cd.rm1;
+            c.lam = (R)lam;
+            c.rm0 = (R)rm0;
+            c.rm1 = (R)rm1;
         }
         for (int m = 0; m < P.M; ++m) {
             ECellT<double> e;
@@ -481,15 +616,23 @@ __device__ inline void c2p(const PT& P, CellT<typename PT::real>& c)
             e.rhok = c.rhok[m];
             e.p = 0.0;
             e.hj2 = c.hj2;
+            e.lam = lam;
+            e.rm0 = rm0;
+            e.rm1 = rm1;
             ent += eos_e_cold(P.d, m, e) + eos_e_shear(P.d, m, e);
             pnt += eos_p_cold(P.d, m, e) + eos_p_shear(P.d, m, e);
             ig += eos_invG(P.d, m, e);
         }
         c.p = (R)(((double)c.E + (double)c.Elo - ked - ent + pnt) / ig);
     } else {
+        if (P.nmix) {  // :104-113
+            c.lam = c.arl / c.arho[0];
+            err = mix_root_find(P, c, ke);
+        }
         c.p = (c.E - ke - eff_e_nonthermal(P, c) + eff_p_nonthermal(P, c)) / (eff_invG(P, c));
     }
     stress(P, c);
+    return err;
 }
 
 // primitiveToConservative (:124-174)
@@ -501,6 +644,14 @@ __device__ inline void p2c(const PT& P, CellT<typename PT::real>& c)
     for (int m = 0; m < P.M; ++m) {
         c.arho[m] = c.alpha[m] * c.rhok[m];
         c.rho += c.arho[m];
+        if (P.nmix && m == 0) {  // :142-147
+            c.arl = c.lam * c.alpha[0] * c.rhok[0];
+            // defineMixtureDensities (equationofstate.cpp:390-396)
+            const R* q = P.prm[0];
+            c.rm0 = c.rhok[0] * (c.lam + (R(1.0) - c.lam) * ((c.p - q[1]) / (c.p - q[5])) *
+                                             ((q[7] * (q[4] - R(1.0))) / (q[3] * (q[0] - R(1.0)))));
+            c.rm1 = (R(1.0) - c.lam) / (R(1.0) / c.rhok[0] - c.lam / c.rm0);
+        }
         if (P.plastic && P.phase[m] == TJ_PHASE_SOLID) c.are[m] = c.eps[m] * c.arho[m];
     }
     hencky(P, c);
@@ -522,7 +673,7 @@ __device__ inline typename PT::real sound_speed(const PT& P, const CellT<typenam
     R a = R(0.0), xit = R(0.0);
     for (int m = 0; m < P.M; ++m) {
         ECellT<R> e = ecell_of(c, m);
-        R xi = R(1.0) / gam(P, m);
+        R xi = eos_xi(P, m, e);
         R v = xi * eos_c2(P, m, e) * c.arho[m] / c.rho;
         a += (R(0.0) < v) ? v : R(0.0);
         xit += xi * c.alpha[m];

@@ -210,6 +210,8 @@ DevParams32 make_params32(const DevParams& DP)
     P.muscl = DP.muscl;
     P.any_solid = DP.any_solid;
     P.radial = DP.radial;
+    P.nmix = DP.nmix;
+    P.reactive = DP.reactive;
     for (int d = 0; d < 3; ++d) {
         P.lo_bc[d] = DP.lo_bc[d];
         P.hi_bc[d] = DP.hi_bc[d];
@@ -224,7 +226,7 @@ DevParams32 make_params32(const DevParams& DP)
     }
 #define CP(f) P.f = DP.f
     CP(S_ALPHA); CP(S_ARHO); CP(S_RHOK); CP(S_RHO); CP(S_RHOU); CP(S_VEL); CP(S_E); CP(S_P); CP(S_V); CP(S_HJ2);
-    CP(S_EPS); CP(S_ARE);
+    CP(S_EPS); CP(S_ARE); CP(S_RMIX); CP(S_LAM); CP(S_ARL); CP(F_ARL); CP(X_ARL);
     CP(F_ALPHA); CP(F_ARHO); CP(F_RHO); CP(F_RHOU); CP(F_VEL); CP(F_E); CP(F_P); CP(F_A); CP(F_SIGMA); CP(F_V);
     CP(F_ARE); CP(NF);
     CP(X_ALPHA); CP(X_ARHO); CP(X_RHOU); CP(X_E); CP(X_SSTAR); CP(X_V); CP(X_VSTAR); CP(X_ARE); CP(NX);

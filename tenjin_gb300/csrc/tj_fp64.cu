@@ -79,7 +79,16 @@ __global__ void k_cell_op(DevParams P, Fp64Bufs b, double* X, const double* X2, 
             // the primitive list carries V; HJ2 recomputed by p2c
         }
         switch (op) {
-            case OP_C2P: c2p(P, c); break;
+            case OP_C2P: {
+                int e = c2p(P, c);
+                if (e) set_status(b.scal, e);
+                break;
+            }
+            case OP_REACTIVE: {
+                int e = reactive_cell(P, c, dt);
+                if (e) set_status(b.scal, e);
+                break;
+            }
             case OP_P2C: p2c(P, c); break;
             case OP_CLEAN_ALPHA: {
                 int e = cleanup_alpha(P, c.alpha);
@@ -102,7 +111,8 @@ __global__ void k_cell_op(DevParams P, Fp64Bufs b, double* X, const double* X2, 
                 double sg[9];
                 for (int q = 0; q < 9; ++q) sg[q] = c.sigma[q];
                 radial_source(P, c, sg, (int)((g - D.off) % D.n[0]), D.dx[0], dt);
-                c2p(P, c);
+                int e = c2p(P, c);
+                if (e) set_status(b.scal, e);
                 break;
             }
             case OP_NAN: {
@@ -150,6 +160,12 @@ __global__ void k_ap_to_state(DevParams P, Fp64Bufs b, int dom, int lx, int ly, 
                 X[(P.S_EPS + m) * nt + g] = APV(P.A_EPS + m);
                 X[(P.S_ARE + m) * nt + g] = APV(P.A_ARE + m);
             }
+        if (P.nmix) {
+            X[P.S_RMIX * nt + g] = APV(P.A_RMIX);
+            X[(P.S_RMIX + 1) * nt + g] = APV(P.A_RMIX + 1);
+            X[P.S_LAM * nt + g] = APV(P.A_LAM);
+            X[P.S_ARL * nt + g] = APV(P.A_ARL);
+        }
 #undef APV
     }
 }
@@ -201,6 +217,12 @@ __global__ void k_state_to_ap(DevParams P, Fp64Bufs b, int dom, int lx, int ly, 
                 APV(P.A_EPS + m) = c.eps[m];
                 APV(P.A_ARE + m) = c.are[m];
             }
+        if (P.nmix) {
+            APV(P.A_RMIX) = c.rm0;
+            APV(P.A_RMIX + 1) = c.rm1;
+            APV(P.A_LAM) = c.lam;
+            APV(P.A_ARL) = c.arl;
+        }
 #undef APV
     }
 }
@@ -222,6 +244,11 @@ __global__ void k_prim_to_state(DevParams P, Fp64Bufs b, int dom, const double* 
             for (int qq = 0; qq < 9; ++qq) c.V[qq] = prim[(w++) * nd + t];
         if (P.plastic)
             for (int m = 0; m < P.M; ++m) c.eps[m] = prim[(w++) * nd + t];
+        if (P.nmix) {  // initialise.cpp:66-71
+            c.lam = prim[(w++) * nd + t];
+            c.rm0 = c.rhok[0];
+            c.rm1 = c.rhok[0];
+        }
         p2c(P, c);
         store_state(P, X, nt, D.off + t, c);
     }

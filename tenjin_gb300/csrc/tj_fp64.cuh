@@ -41,7 +41,7 @@ int fp64_set_dt(const Fp64Bufs& b, double dt, cudaStream_t st);
 
 // Whole-array operators of the C ABI.
 enum CellOp { OP_C2P = 0, OP_P2C = 1, OP_CLEAN_ALPHA = 2, OP_CLEAN_V = 3, OP_PLASTIC = 4, OP_NAN = 5, OP_AVERAGE = 6,
-              OP_RADIAL = 7 };
+              OP_RADIAL = 7, OP_REACTIVE = 8 };
 int fp64_cell_op(const DevParams& P, const Fp64Bufs& b, double* X, const double* X2, int op, cudaStream_t st,
                  double dt = 0.0);
 

@@ -140,6 +140,12 @@ __device__ inline void load_state(const PT& P, const R* X, long long nt, long lo
             c.eps[m] = X[(P.S_EPS + m) * nt + g];
             c.are[m] = X[(P.S_ARE + m) * nt + g];
         }
+    if (P.nmix) {
+        c.rm0 = X[P.S_RMIX * nt + g];
+        c.rm1 = X[(P.S_RMIX + 1) * nt + g];
+        c.lam = X[P.S_LAM * nt + g];
+        c.arl = X[P.S_ARL * nt + g];
+    }
 }
 
 template <typename PT, typename R = typename PT::real>
@@ -169,6 +175,12 @@ __device__ inline void store_state(const PT& P, R* X, long long nt, long long g,
             X[(P.S_EPS + m) * nt + g] = c.eps[m];
             X[(P.S_ARE + m) * nt + g] = c.are[m];
         }
+    if (P.nmix) {
+        X[P.S_RMIX * nt + g] = c.rm0;
+        X[(P.S_RMIX + 1) * nt + g] = c.rm1;
+        X[P.S_LAM * nt + g] = c.lam;
+        X[P.S_ARL * nt + g] = c.arl;
+    }
 }
 
 template <typename PT, typename R = typename PT::real>
@@ -196,6 +208,7 @@ __device__ inline void store_face(const PT& P, R* F, long long nt, long long g, 
     }
     if (P.plastic)
         for (int m = 0; m < P.M; ++m) F[(P.F_ARE + m) * nt + g] = c.are[m];
+    if (P.nmix) F[P.F_ARL * nt + g] = c.arl;
 }
 
 template <typename PT, typename R = typename PT::real>
@@ -232,6 +245,7 @@ __device__ inline void load_face(const PT& P, const R* F, long long nt, long lon
     }
     if (P.plastic)
         for (int m = 0; m < P.M; ++m) c.are[m] = F[(P.F_ARE + m) * nt + g];
+    if (P.nmix) c.arl = F[P.F_ARL * nt + g];
 }
 
 template <typename R>
@@ -361,6 +375,7 @@ __global__ void k_recon(PT P, PathBufs<typename PT::real> b, const R* __restrict
                 for (int qq = 0; qq < 9; ++qq) muscl1(um.V[qq], u0.V[qq], up.V[qq], L.V[qq], Rc.V[qq]);
             if (P.plastic)
                 for (int m = 0; m < P.M; ++m) muscl1(um.eps[m], u0.eps[m], up.eps[m], L.eps[m], Rc.eps[m]);
+            if (P.nmix) muscl1(um.lam, u0.lam, up.lam, L.lam, Rc.lam);
         }
         int reps = 0;
         if (P.thinc) {
@@ -469,6 +484,7 @@ __device__ inline void star_state(const PT& P, const CellT<R>& U, CellT<R>& Us, 
         Us.alpha[m] = U.alpha[m];
         Us.arho[m] = mult * U.arho[m];
         Us.rhok[m] = Us.arho[m] / Us.alpha[m];
+        if (P.nmix && m == 0) Us.arl = mult * U.arl;
         if (P.plastic && P.phase[m] == TJ_PHASE_SOLID) Us.are[m] = mult * U.are[m];
         Us.rho += Us.arho[m];
     }
@@ -509,6 +525,7 @@ __device__ inline void phys_flux(const PT& P, const CellT<R>& U, int d, R* F)
         }
     if (P.plastic)
         for (int m = 0; m < P.M; ++m) F[P.X_ARE + m] = U.are[m] * ud;
+    if (P.nmix) F[P.X_ARL] = U.arl * ud;
 }
 
 // Conservative values of a state in the flux-word layout.
@@ -527,6 +544,7 @@ __device__ inline void cons_vals(const PT& P, const CellT<R>& U, R* Q)
         for (int q = 0; q < 9; ++q) Q[P.X_V + q] = U.V[q];
     if (P.plastic)
         for (int m = 0; m < P.M; ++m) Q[P.X_ARE + m] = U.are[m];
+    if (P.nmix) Q[P.X_ARL] = U.arl;
 }
 
 #define TJ_MAXX 32
@@ -838,7 +856,35 @@ __device__ inline bool cell_has_nan(const PT& P, const CellT<R>& c)
         for (int q = 0; q < 9; ++q) n |= isnan(c.V[q]);
     if (P.plastic)
         for (int m = 0; m < P.M; ++m) n |= isnan(c.eps[m]) || isnan(c.are[m]);
+    if (P.nmix) n |= isnan(c.lam) || isnan(c.arl);
     return n;
+}
+
+// pressureBased_UpdateMassFraction (reactive.cpp:3-26) for the mixture
+// (material 0): alphaRhoLambda after one Euler step of the pressure-based burn
+// d(alpha rho lambda)/dt = -20 (alpha rho)^0.5 (alpha rho lambda)^0.5 (p/1e6)^1.2,
+// clipped at 0; cells with alpha < 0.5 keep their value.
+template <typename R>
+__device__ __forceinline__ R reactive_euler(R arl, R arho, R p, R alpha, R dt)
+{
+    const R sigma = R(20.0), nu = R(0.5), n = R(1.2);
+    if (alpha < R(0.5)) return arl;
+    R r = arl - (dt) * (sigma * tjm_pow(arho, R(1.0) - nu) * tjm_pow(arl, nu) * tjm_pow((p / R(1E6)), n));
+    if (r < R(0.0)) r = R(0.0);
+    return r;
+}
+
+// reactiveUpdate (reactive.cpp:60-103) on one cell: two Euler steps from the
+// same alphaRho, pressure and alpha, averaged with the start value, then
+// conservativeToPrimitive. Returns the c2p status.
+template <typename PT, typename R = typename PT::real>
+__device__ inline int reactive_cell(const PT& P, CellT<R>& c, R dt)
+{
+    const R a0 = c.arl;
+    const R a1 = reactive_euler(a0, c.arho[0], c.p, c.alpha[0], dt);
+    const R a2 = reactive_euler(a1, c.arho[0], c.p, c.alpha[0], dt);
+    c.arl = (a0 * (R(1.0) / R(2.0))) + (a2 * (R(1.0) / R(2.0)));
+    return c2p(P, c);
 }
 
 // addGeometricSourceTerm (radial.cpp:5-31) on one cell: every conservative
@@ -865,6 +911,7 @@ __device__ inline void radial_source(const PT& P, CellT<R>& c, const R* sg, int 
     for (int r = 0; r < 3; ++r) vds += c.vel[r] * sg[3 * r];
     if constexpr (sizeof(R) == 4) dd_add32(c.E, c.Elo, s * ((c.E * u) - vds));
     else c.E += s * ((c.E * u) - vds);
+    if (P.nmix) c.arl += s * (c.arl * u);
     if (P.solid) {
 #pragma unroll
         for (int q = 0; q < 9; ++q) {
@@ -921,9 +968,11 @@ __global__ void k_update(PT P, PathBufs<typename PT::real> b, const R* __restric
             }
         if (P.plastic)
             for (int m = 0; m < P.M; ++m) Yc.are[m] += dtdx * (FXW(P.X_ARE + m, f0) - FXW(P.X_ARE + m, f1));
+        if (P.nmix) Yc.arl += dtdx * (FXW(P.X_ARL, f0) - FXW(P.X_ARL, f1));
 #undef FXW
         if (last) {
-            c2p(P, Yc);
+            const int ce = c2p(P, Yc);
+            if (ce) set_status(b.scal, ce);
             if (finish) {
                 const R p_stage = Yc.p;  // U2's pressure, before the average
                 // U1 = U*0.5 + U2*0.5 over every carried component (hllc.cpp:705)
@@ -952,9 +1001,19 @@ __global__ void k_update(PT P, PathBufs<typename PT::real> b, const R* __restric
                     for (int qq = 0; qq < 9; ++qq) Yc.V[qq] = (A0.V[qq] * (R(1.0) / R(2.0))) + (Yc.V[qq] * (R(1.0) / R(2.0)));
                     Yc.hj2 = (A0.hj2 * (R(1.0) / R(2.0))) + (Yc.hj2 * (R(1.0) / R(2.0)));
                 }
+                if (P.nmix) {
+                    Yc.rm0 = (A0.rm0 * (R(1.0) / R(2.0))) + (Yc.rm0 * (R(1.0) / R(2.0)));
+                    Yc.rm1 = (A0.rm1 * (R(1.0) / R(2.0))) + (Yc.rm1 * (R(1.0) / R(2.0)));
+                    Yc.lam = (A0.lam * (R(1.0) / R(2.0))) + (Yc.lam * (R(1.0) / R(2.0)));
+                    Yc.arl = (A0.arl * (R(1.0) / R(2.0))) + (Yc.arl * (R(1.0) / R(2.0)));
+                }
                 if (finish == 2) {  // advance() alone: the average only
                     store_state(P, b.A, nt, g, Yc);
                     continue;
+                }
+                if (P.reactive && P.nmix) {  // main.cpp:149-152
+                    const int re = reactive_cell(P, Yc, dtdx_num);
+                    if (re) set_status(b.scal, re);
                 }
                 if (P.plastic) {
                     int e;
@@ -980,7 +1039,8 @@ __global__ void k_update(PT P, PathBufs<typename PT::real> b, const R* __restric
                                                              ((-p_stage * dl) * (R(1.0) / R(2.0)));
                         }
                     radial_source(P, Yc, sg, i, D.dx[0], dtdx_num);
-                    c2p(P, Yc);  // geometricSourceTerm (radial.cpp:50)
+                    const int rc = c2p(P, Yc);  // geometricSourceTerm (radial.cpp:50)
+                    if (rc) set_status(b.scal, rc);
                 }
                 if (P.solid) cleanup_v_cell(P, Yc);
                 int e = cleanup_alpha(P, Yc.alpha);

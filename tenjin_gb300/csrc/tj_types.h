@@ -14,6 +14,8 @@ struct DevParams {
     int dim, M, solid, thinc, plastic, muscl, any_solid;
     int fused64;  // fused kernels in binary64 (TJ_PRECISION_FUSED64)
     int radial;   // RADIAL: geometric source term after the plastic update
+    int nmix;     // numberOfMixtures (0 or 1; material 0 holds the MixtureEOS)
+    int reactive; // REACTIVE: reactiveUpdate after advance
     int lo_bc[3], hi_bc[3];
     double cfl, beta;
     int phase[TJ_MAX_MAT], eos[TJ_MAX_MAT];
@@ -21,13 +23,17 @@ struct DevParams {
     double yield[TJ_MAX_MAT];
     // carried state (one SoA block of ntot cells per word)
     int S_ALPHA, S_ARHO, S_RHOK, S_RHO, S_RHOU, S_VEL, S_E, S_P, S_V, S_HJ2, S_EPS, S_ARE, NS;
+    int S_RMIX, S_LAM, S_ARL;  // mixture: rhomix (2), lambda, alphaRhoLambda; -1 without
     // reconstructed face state (UL / UR)
     int F_ALPHA, F_ARHO, F_RHO, F_RHOU, F_VEL, F_E, F_P, F_A, F_SIGMA, F_V, F_ARE, NF;
+    int F_ARL;
     // face flux
     int X_ALPHA, X_ARHO, X_RHOU, X_E, X_SSTAR, X_V, X_VSTAR, X_ARE, NX;
+    int X_ARL;
     // AccessPattern (reference component order)
     int A_ALPHA, A_ARHO, A_RHOK, A_RHO, A_RHOU, A_VEL, A_E, A_P, A_A, A_USTAR, A_SIGMA, A_V, A_VSTAR, A_DEVH, A_HJ2,
         A_EPS, A_ARE, NCOMP;
+    int A_RMIX, A_LAM, A_ARL;
     int S_ELO;  // binary32 state only (the low word of the energy); -1 here
 };
 
@@ -39,14 +45,18 @@ struct DevParams32 {
     int dim, M, solid, thinc, plastic, muscl, any_solid;
     int fused64;
     int radial;
+    int nmix, reactive;
     int lo_bc[3], hi_bc[3];
     float cfl, beta;
     int phase[TJ_MAX_MAT], eos[TJ_MAX_MAT];
     float prm[TJ_MAX_MAT][TJ_MAX_EOS_PARAMS];
     float yield[TJ_MAX_MAT];
     int S_ALPHA, S_ARHO, S_RHOK, S_RHO, S_RHOU, S_VEL, S_E, S_P, S_V, S_HJ2, S_EPS, S_ARE, NS;
+    int S_RMIX, S_LAM, S_ARL;
     int F_ALPHA, F_ARHO, F_RHO, F_RHOU, F_VEL, F_E, F_P, F_A, F_SIGMA, F_V, F_ARE, NF;
+    int F_ARL;
     int X_ALPHA, X_ARHO, X_RHOU, X_E, X_SSTAR, X_V, X_VSTAR, X_ARE, NX;
+    int X_ARL;
     int S_ELO;
     DevParams d;
 };

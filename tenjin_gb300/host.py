@@ -41,9 +41,9 @@ def _dp(a: np.ndarray):
 
 def make_params(case: Case, precision: int = FP64) -> _lib.TjParams:
     p = _lib.TjParams()
-    p.dim, p.n_materials, p.n_mixtures = case.dim, case.M, 0
-    p.SOLID, p.THINC, p.RADIAL, p.PLASTIC, p.REACTIVE, p.MUSCL = (case.solid, case.thinc, getattr(case, "radial", 0),
-                                                                  case.plastic, 0, case.muscl)
+    p.dim, p.n_materials, p.n_mixtures = case.dim, case.M, case.nmix
+    p.SOLID, p.THINC, p.RADIAL, p.PLASTIC, p.REACTIVE, p.MUSCL = (case.solid, case.thinc, case.radial,
+                                                                  case.plastic, case.reactive, case.muscl)
     p.nghost = case.nghost
     for d in range(3):
         p.lo_bc[d], p.hi_bc[d] = case.lo_bc[d], case.hi_bc[d]
@@ -136,6 +136,10 @@ class TenjinGPU:
 
     def plasticUpdate(self, dt: float = 0.0):
         self._check(self.L.tj_plastic_update(self.h, float(dt)))
+
+    def reactiveUpdate(self, dt: float):
+        """reactiveUpdate (reactive.cpp:60-103) with parameters.dt = dt."""
+        self._check(self.L.tj_reactive_update(self.h, float(dt)))
 
     def geometricSourceTerm(self, dt: float):
         """geometricSourceTerm (radial.cpp:37-54) with parameters.dt = dt."""

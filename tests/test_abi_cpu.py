@@ -43,7 +43,7 @@ def test_library_targets_sm_103a():
 @pytest.mark.parametrize("mutate,why", [
     (lambda p: setattr(p, "dim", 4), "dim must be"),
     (lambda p: setattr(p, "n_mixtures", 1), "mixtures"),
-    (lambda p: setattr(p, "REACTIVE", 1), "REACTIVE"),
+    (lambda p: setattr(p, "precision", 7), "unknown precision"),
     (lambda p: setattr(p, "nghost", 1), "nghost"),
     (lambda p: setattr(p, "n_materials", 5), "n_materials"),
 ])
@@ -66,9 +66,31 @@ def test_create_rejects_radial_with_elastic_solids(lib, capfd):
     assert "RADIAL with elastic solids" in capfd.readouterr().err
 
 
-@pytest.mark.parametrize("case", ["sod", "plastic"])
-def test_create_accepts_radial_fluids_and_plastic_solids(lib, capfd, case):
-    c = cases.sod_1d(ncells=10) if case == "sod" else cases.solid_mixture_2d(n=8)
+@pytest.mark.parametrize("mutate,why", [
+    (lambda c: setattr(c, "materials", c.materials[::-1]), "material 0"),
+    (lambda c: setattr(c, "solid", 1), "SOLID"),
+])
+def test_create_rejects_unsupported_mixtures(lib, capfd, mutate, why):
+    c = cases.reactive_charge(dim=1, n=10)
+    mutate(c)
+    p = make_params(c)
+    h = ctypes.c_void_p()
+    assert lib.tj_create(ctypes.byref(p), ctypes.byref(h)) == -1
+    assert why in capfd.readouterr().err
+
+
+def test_create_rejects_two_mixtures(lib, capfd):
+    p = make_params(cases.reactive_charge(dim=1, n=10))
+    p.n_mixtures = 2
+    h = ctypes.c_void_p()
+    assert lib.tj_create(ctypes.byref(p), ctypes.byref(h)) == -1
+    assert "n_mixtures must be 0 or 1" in capfd.readouterr().err
+
+
+@pytest.mark.parametrize("case", ["sod", "plastic", "reactive"])
+def test_create_accepts_radial_fluids_plastic_solids_and_mixtures(lib, capfd, case):
+    c = (cases.sod_1d(ncells=10) if case == "sod" else cases.solid_mixture_2d(n=8) if case == "plastic"
+         else cases.reactive_charge(dim=2, n=8))
     c.radial = 1
     p = make_params(c)
     h = ctypes.c_void_p()

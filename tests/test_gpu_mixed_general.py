@@ -79,3 +79,13 @@ def test_radial_source(geom):
     l1, _, cfg = compare(c, c.max_steps)
     assert "binary32 per-direction" in cfg
     assert l1 <= L1_TOL, l1
+
+
+@pytest.mark.parametrize("dim", [1, 2])
+def test_mixture_and_reactive_update(dim):
+    """MixtureEOS with the bisection closure in binary64 and the burn in binary32."""
+    c = cases.reactive_charge(dim=dim, n=200 if dim == 1 else 48, max_grid_size=50 if dim == 1 else 16,
+                              max_steps=120 if dim == 1 else 40)
+    l1, _, cfg = compare(c, c.max_steps)
+    assert "binary32 per-direction" in cfg
+    assert l1 <= L1_TOL, l1

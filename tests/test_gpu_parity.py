@@ -99,6 +99,25 @@ def test_radial_operators_one_by_one(name):
     assert fx.rel_diff(g.state(0)[idx], ref["states"][0][idx]) <= TOL
 
 
+def test_reactive_operators_one_by_one():
+    """getTimeStep, advance, reactiveUpdate, cleanUpAlpha as separate calls
+    reproduce the port's steps on the MixtureEOS charge."""
+    c = fx.build_case("reactive_charge_1d")
+    c.max_steps = 8
+    g = TenjinGPU(c)
+    ref = port.run_port(c)
+    for n in range(c.max_steps):
+        dt = g.getTimeStep()
+        if n < 5:
+            dt *= 0.2
+        assert abs(dt - ref["dts"][n]) <= TOL * dt
+        g.advance(dt)
+        g.reactiveUpdate(dt)
+        g.cleanUpAlpha()
+    idx = carried_components(c)
+    assert fx.rel_diff(g.state(0)[idx], ref["states"][0][idx]) <= TOL
+
+
 def test_fab_exchange_roundtrip_keeps_ghosts():
     c = cases.shock_bubble_2d(n=24, max_grid_size=10, max_steps=1)
     g = TenjinGPU(c)
