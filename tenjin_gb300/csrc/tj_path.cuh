@@ -1026,15 +1026,17 @@ __global__ void k_update(PT P, PathBufs<typename PT::real> b, const R* __restric
                 }
                 if (P.radial) {
                     // the stress the reference's U1 holds here: fresh from the
-                    // plastic update's c2p, else the average of U's and U2's
-                    // (fluids only: -p I each, boxaccesscellarray.cpp:204-212)
+                    // c2p of the plastic or the reactive update, else the
+                    // average of U's and U2's (fluids only: -p I each,
+                    // boxaccesscellarray.cpp:204-212)
+                    const bool fresh = P.plastic || (P.reactive && P.nmix);
                     R sg[9];
 #pragma unroll
                     for (int r = 0; r < 3; ++r)
 #pragma unroll
                         for (int qq = 0; qq < 3; ++qq) {
                             const R dl = (R)(r == qq);
-                            sg[3 * r + qq] = P.plastic ? Yc.sigma[3 * r + qq]
+                            sg[3 * r + qq] = fresh ? Yc.sigma[3 * r + qq]
                                                        : ((-A0.p * dl) * (R(1.0) / R(2.0))) +
                                                              ((-p_stage * dl) * (R(1.0) / R(2.0)));
                         }

@@ -13,9 +13,10 @@ keys the reference reads onto a :class:`~tenjin_gb300.cases.Case`:
 * listOfMaterials (getMaterialParameters, initialise.cpp:125-235): material
   ("solid"/"fluid"), EOS ("MieGruneisen", "RomenskiiSolid", "WilkinsSolid"),
   adiabaticIndex, pref, eref, CV, then rho0 K0 EOSalpha EOSbeta (Romenskii) or
-  rho0 e1..e5 (Wilkins), G0 for solids, yieldStress when PLASTIC;
-* listOfStates (getState, initialise.cpp:237-267): per material alpha, rho
-  and F[9] (solids), then p, u, v, w.
+  rho0 e1..e5 (Wilkins), G0 for solids, yieldStress when PLASTIC; a fluid with
+  mixture = 1 is a MixtureEOS with adiabaticIndexmix, prefmix, erefmix, CVmix;
+* listOfStates (getState, initialise.cpp:237-267): per material alpha, rho,
+  lambda (the mixture) and F[9] (solids), then p, u, v, w.
 
 The reference chooses the state of each cell with a hard-coded geometry
 (chooseStateBasedOnInitialCondition, initialise.cpp:387-): ``to_case`` takes
@@ -153,9 +154,14 @@ def materials(cfg: Dict[str, Any]) -> List[Material]:
         eos = mat.get("EOS")
         if eos not in _EOS:
             raise SettingsError(f"No valid EOS selected for material {m}")
-        if mat.get("mixture", 0):
-            raise SettingsError("mixtures (MixtureEOS) are not supported")
+        mix = int(mat.get("mixture", 0))
         prm = [float(mat["adiabaticIndex"]), float(mat["pref"]), float(mat["eref"]), float(mat["CV"])]
+        if mix:
+            if eos != "MieGruneisen" or mat.get("material") == "solid":
+                raise SettingsError("Error: solid can't be a mixture (atm)")
+            prm += [float(mat[k]) for k in ("adiabaticIndexmix", "prefmix", "erefmix", "CVmix")]
+            out.append(Material(cases.PHASE_FLUID, cases.EOS_MIXTURE, prm, 0.0))
+            continue
         if eos == "RomenskiiSolid":
             prm += [float(mat[k]) for k in ("rho0", "K0", "EOSalpha", "EOSbeta")]
         elif eos == "WilkinsSolid":
@@ -185,11 +191,11 @@ def to_case(cfg: Dict[str, Any], dim: int, max_grid_size: int,
     M = len(mats)
     c = Case("settings", dim, mats, solid=int(cfg.get("SOLID", 0)), thinc=int(cfg.get("THINC", 0)),
              plastic=int(cfg.get("PLASTIC", 0)), muscl=int(cfg.get("MUSCL", 1)), nghost=nghost,
-             radial=int(cfg.get("RADIAL", 0)),
+             radial=int(cfg.get("RADIAL", 0)), reactive=int(cfg.get("REACTIVE", 0)),
              cfl=float(cfg["CFL"]), thinc_beta=float(cfg.get("THINCbeta", 1.6)),
              final_t=float(cfg["finalTime"]))
-    if int(cfg.get("mixtures", 0)) or int(cfg.get("REACTIVE", 0)):
-        raise SettingsError("mixtures and REACTIVE are not supported")
+    if int(cfg.get("mixtures", 0)) != c.nmix:
+        raise SettingsError("mixtures must equal the number of materials with mixture = 1")
     axes = "xyz"
     n = [int(cfg[f"numberOf{axes[d]}Cells"]) if d < dim else 1 for d in range(3)]
     L = [float(cfg[f"{axes[d]}domainLength"]) if d < dim else 1.0 for d in range(3)]
@@ -222,6 +228,8 @@ def to_case(cfg: Dict[str, Any], dim: int, max_grid_size: int,
         prim[2 * M + 1][msk] = float(st.get("v", 0.0))
         prim[2 * M + 2][msk] = float(st.get("w", 0.0))
         prim[2 * M + 3][msk] = float(st["p"])
+        if c.nmix:  # initialise.cpp:66-71, 245-248
+            prim[c.nprim - 1][msk] = float(st["material"][0]["lambda"])
     if c.solid:
         for r in range(3):
             prim[2 * M + 4 + 3 * r + r] = 1.0
@@ -231,6 +239,13 @@ def to_case(cfg: Dict[str, Any], dim: int, max_grid_size: int,
     for m, mat in enumerate(mats):
         a, rk, q = prim[m], prim[M + m], mat.params
         G = q[0] - 1.0
+        if mat.eos == cases.EOS_MIXTURE:
+            # rhomix = rho_k at this point (initialise.cpp:68-69), so the
+            # density ratios of equationofstate.cpp:167-171 are 1
+            lam = prim[c.nprim - 1]
+            pc += (q[1] * a / (q[0] - 1.0)) * lam * rk / rk + (q[5] * a / (q[4] - 1.0)) * (1.0 - lam) * rk / rk
+            ig += a / ((lam * q[0] * q[3] + (1.0 - lam) * q[4] * q[7]) / (lam * q[3] + (1.0 - lam) * q[7]) - 1.0)
+            continue
         if mat.eos == cases.EOS_MIEGRUNEISEN:
             pc += q[1] * a / G
         elif mat.eos == cases.EOS_ROMENSKII:

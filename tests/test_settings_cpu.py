@@ -69,9 +69,31 @@ def test_to_case_carries_radial():
     assert settings.to_case(settings.parse(DECK), 1, 50).radial == 0
 
 
+def test_to_case_maps_a_mixture_and_reactive():
+    cfg = settings.parse(DECK)
+    cfg["mixtures"], cfg["REACTIVE"] = 1, 1
+    m0 = cfg["listOfMaterials"][0]
+    m0["mixture"] = 1
+    m0.update({"adiabaticIndexmix": 1.4, "prefmix": 0.0, "erefmix": 0.0, "CVmix": 1000.0})
+    for st, lam in zip(cfg["listOfStates"], (0.7, 0.999)):
+        st["material"][0]["lambda"] = lam
+    c = settings.to_case(cfg, 1, 50)
+    assert c.nmix == 1 and c.reactive == 1
+    assert c.materials[0].eos == cases.EOS_MIXTURE
+    assert c.materials[0].params == [4.4, -2.64e9, 0.0, 1.0, 1.4, 0.0, 0.0, 1000.0]
+    d = c.domains[0]
+    assert d.prim.shape[0] == c.nprim
+    assert np.all(d.prim[-1, 0, 0, :50] == 0.7) and np.all(d.prim[-1, 0, 0, 50:] == 0.999)
+    # initialise.cpp:104 with rhomix = rho_k: p += sum p_cold / sum alpha/Gamma
+    a0, lam = 0.999999, 0.7
+    g = (lam * 4.4 * 1.0 + (1 - lam) * 1.4 * 1000.0) / (lam * 1.0 + (1 - lam) * 1000.0) - 1.0
+    pc = (-2.64e9 * a0 / 3.4) * lam
+    assert d.prim[2 * 2 + 3, 0, 0, 0] == pytest.approx(1.0e9 + pc / (a0 / g + (1 - a0) / 0.4), rel=1e-12)
+
+
 def test_to_case_rejects_what_the_path_does_not_cover():
     cfg = settings.parse(DECK)
-    cfg["REACTIVE"] = 1
+    cfg["mixtures"] = 1  # no material has mixture = 1
     with pytest.raises(settings.SettingsError):
         settings.to_case(cfg, 1, 50)
     cfg = settings.parse(DECK)
