@@ -102,8 +102,20 @@ struct Sm3 {
     static constexpr int F_OFF = C_OFF + NC * CV;
     static constexpr int RED_OFF = F_OFF + NF * FV;
     static constexpr int TOTAL = RED_OFF + 64;
-    static constexpr size_t BYTES = sizeof(float) * TOTAL;
+    // a second staging buffer (primitives and conserved words) after TOTAL:
+    // the next tile's copies land there while this tile computes
+    static constexpr size_t BYTES = sizeof(float) * (TOTAL + F_OFF);
 };
+
+// Asynchronous 4-byte global -> shared copies (cp.async, completed in groups).
+__device__ __forceinline__ void cp_async4(float* dst, const float* src)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int NG>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(NG) : "memory"); }
 
 __device__ __forceinline__ int map3(int i, int n, int lo, int hi, bool& refl)
 {
@@ -285,6 +297,82 @@ __device__ __forceinline__ void recon3(const M3P& P, const float* sm, int s, int
     p2c3<M>(P, rk, S);
 }
 
+// Issue the copies of one tile's staged primitives (tile + 2-cell halo,
+// ghosts at their boundary images) and of its output cells' conserved words
+// into the staging buffer at sp. Values arrive unmodified: stage_fix negates
+// the reflected velocities once they have landed.
+template <int M, int TX, int TY, int TZ>
+__device__ void stage_issue(const M3P& P, const Work3& w, const Dom3& D, const float* __restrict__ Xin, long long N,
+                            float* sp)
+{
+    using SM = Sm3<M, TX, TY, TZ>;
+    const int ex = w.ex, ey = w.ey, ez = w.ez, i0 = w.i0, j0 = w.j0, k0 = w.k0;
+    const int nx = D.n[0], ny = D.n[1], nz = D.n[2];
+    const long long off = D.off;
+    const int sx = ex + 4, sy = ey + 4, sz = ez + 4;
+    for (int t = threadIdx.x; t < sx * sy * sz; t += NT3) {
+        const int x = t % sx, y = (t / sx) % sy, z = t / (sx * sy);
+        bool rx, ry, rz;
+        const int gi = map3(i0 - 2 + x, nx, P.lo_bc[0], P.hi_bc[0], rx);
+        const int gj = map3(j0 - 2 + y, ny, P.lo_bc[1], P.hi_bc[1], ry);
+        const int gk = map3(k0 - 2 + z, nz, P.lo_bc[2], P.hi_bc[2], rz);
+        const long long g = off + gi + (long long)nx * (gj + (long long)ny * gk);
+        const int s = x + SM::SX * (y + SM::SY * z);
+#pragma unroll
+        for (int m = 0; m < M; ++m) {
+            cp_async4(sp + SM::P_OFF + m * SM::SV + s, Xin + S3_A<M>(m) * N + g);
+            cp_async4(sp + SM::P_OFF + (M + m) * SM::SV + s, Xin + S3_RK<M>(m) * N + g);
+        }
+#pragma unroll
+        for (int r = 0; r < 3; ++r) cp_async4(sp + SM::P_OFF + (2 * M + r) * SM::SV + s, Xin + S3_U<M>(r) * N + g);
+        cp_async4(sp + SM::P_OFF + (2 * M + 3) * SM::SV + s, Xin + S3_P<M>() * N + g);
+    }
+    for (int t = threadIdx.x; t < ex * ey * ez; t += NT3) {
+        const int x = t % ex, y = (t / ex) % ey, z = t / (ex * ey);
+        const long long g = off + (i0 + x) + (long long)nx * ((j0 + y) + (long long)ny * (k0 + z));
+        const int c = x + TX * (y + TY * z);
+#pragma unroll
+        for (int m = 0; m < M; ++m) {
+            cp_async4(sp + SM::C_OFF + m * SM::CV + c, Xin + S3_A<M>(m) * N + g);
+            cp_async4(sp + SM::C_OFF + (M + m) * SM::CV + c, Xin + S3_AR<M>(m) * N + g);
+        }
+#pragma unroll
+        for (int r = 0; r < 3; ++r) cp_async4(sp + SM::C_OFF + (2 * M + r) * SM::CV + c, Xin + S3_RU<M>(r) * N + g);
+        cp_async4(sp + SM::C_OFF + (2 * M + 3) * SM::CV + c, Xin + S3_EH<M>() * N + g);
+        cp_async4(sp + SM::C_OFF + (2 * M + 4) * SM::CV + c, Xin + S3_EL<M>() * N + g);
+    }
+}
+
+// The reflect_odd ghosts (FillDomainBoundary) of a landed staging buffer:
+// negate the velocity normal to each reflective face the ghost crosses.
+// Returns whether the tile reaches a reflective face (the same answer in
+// every thread of the block).
+template <int M, int TX, int TY, int TZ>
+__device__ bool stage_fix(const M3P& P, const Work3& w, const Dom3& D, float* sp)
+{
+    using SM = Sm3<M, TX, TY, TZ>;
+    const int lo[3] = {w.i0, w.j0, w.k0}, ext[3] = {w.ex, w.ey, w.ez};
+    bool near = false;
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+        near |= (P.lo_bc[d] == TJ_BC_REFLECTIVE && lo[d] < 2) ||
+                (P.hi_bc[d] == TJ_BC_REFLECTIVE && lo[d] + ext[d] + 2 > D.n[d]);
+    if (!near) return false;
+    const int sx = w.ex + 4, sy = w.ey + 4, sz = w.ez + 4;
+    for (int t = threadIdx.x; t < sx * sy * sz; t += NT3) {
+        const int x = t % sx, y = (t / sx) % sy, z = t / (sx * sy);
+        bool r3[3];
+        map3(w.i0 - 2 + x, D.n[0], P.lo_bc[0], P.hi_bc[0], r3[0]);
+        map3(w.j0 - 2 + y, D.n[1], P.lo_bc[1], P.hi_bc[1], r3[1]);
+        map3(w.k0 - 2 + z, D.n[2], P.lo_bc[2], P.hi_bc[2], r3[2]);
+        const int s = x + SM::SX * (y + SM::SY * z);
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+            if (r3[r]) sp[SM::P_OFF + (2 * M + r) * SM::SV + s] = -sp[SM::P_OFF + (2 * M + r) * SM::SV + s];
+    }
+    return true;
+}
+
 template <int M, int TX, int TY, int TZ>
 __global__ void __launch_bounds__(NT3) k_stage3d(M3P P, M3B b, int stage, int force)
 {
@@ -298,57 +386,40 @@ __global__ void __launch_bounds__(NT3) k_stage3d(M3P P, M3B b, int stage, int fo
     const float dtf = (float)b.scal->dt;
     float dtmin = 3.0e38f;
     bool nan_seen = false;
-    __shared__ Work3 w;
-    __shared__ Dom3 D;
+    __shared__ Work3 wsh[2];
+    __shared__ Dom3 Dsh[2];
 
-    for (int wi = blockIdx.x; wi < b.nwork; wi += gridDim.x) {
-        __syncthreads();  // the previous tile is done with shared memory
+    int wi = blockIdx.x;
+    if (wi < b.nwork) {
         if (threadIdx.x == 0) {
-            w = b.work[wi];
-            D = b.doms[w.dom];
+            wsh[0] = b.work[wi];
+            Dsh[0] = b.doms[wsh[0].dom];
         }
         __syncthreads();
+        stage_issue<M, TX, TY, TZ>(P, wsh[0], Dsh[0], Xin, N, sm);
+    }
+    cp_async_commit();
+    for (int it = 0; wi < b.nwork; wi += gridDim.x, ++it) {
+        const int cur = it & 1, nxt = cur ^ 1;
+        float* const sp = sm + (cur ? SM::TOTAL : 0);  // this tile's staging buffer
+        const int wn = wi + gridDim.x;
+        __syncthreads();  // the previous tile is done with the other buffer and its slot
+        if (threadIdx.x == 0 && wn < b.nwork) {
+            wsh[nxt] = b.work[wn];
+            Dsh[nxt] = b.doms[wsh[nxt].dom];
+        }
+        __syncthreads();
+        if (wn < b.nwork) stage_issue<M, TX, TY, TZ>(P, wsh[nxt], Dsh[nxt], Xin, N, sm + (nxt ? SM::TOTAL : 0));
+        cp_async_commit();
+        cp_async_wait<1>();  // this tile's copies have landed
+        __syncthreads();
+        if (stage_fix<M, TX, TY, TZ>(P, wsh[cur], Dsh[cur], sp)) __syncthreads();
+        const Work3& w = wsh[cur];
+        const Dom3& D = Dsh[cur];
         const int ex = w.ex, ey = w.ey, ez = w.ez;
         const int i0 = w.i0, j0 = w.j0, k0 = w.k0;
         const long long off = D.off;
         const int nx = D.n[0], ny = D.n[1], nz = D.n[2];
-        // ---- stage primitives of tile + halo (ghosts: boundary images) ----
-        const int sx = ex + 4, sy = ey + 4, sz = ez + 4;
-        for (int t = threadIdx.x; t < sx * sy * sz; t += NT3) {
-            const int x = t % sx, y = (t / sx) % sy, z = t / (sx * sy);
-            bool rx, ry, rz;
-            const int gi = map3(i0 - 2 + x, nx, P.lo_bc[0], P.hi_bc[0], rx);
-            const int gj = map3(j0 - 2 + y, ny, P.lo_bc[1], P.hi_bc[1], ry);
-            const int gk = map3(k0 - 2 + z, nz, P.lo_bc[2], P.hi_bc[2], rz);
-            const long long g = off + gi + (long long)nx * (gj + (long long)ny * gk);
-            const int s = x + SM::SX * (y + SM::SY * z);
-#pragma unroll
-            for (int m = 0; m < M; ++m) {
-                sm[SM::P_OFF + m * SM::SV + s] = Xin[S3_A<M>(m) * N + g];
-                sm[SM::P_OFF + (M + m) * SM::SV + s] = Xin[S3_RK<M>(m) * N + g];
-            }
-            const float u = Xin[S3_U<M>(0) * N + g], v = Xin[S3_U<M>(1) * N + g], ww = Xin[S3_U<M>(2) * N + g];
-            sm[SM::P_OFF + (2 * M) * SM::SV + s] = rx ? -u : u;
-            sm[SM::P_OFF + (2 * M + 1) * SM::SV + s] = ry ? -v : v;
-            sm[SM::P_OFF + (2 * M + 2) * SM::SV + s] = rz ? -ww : ww;
-            sm[SM::P_OFF + (2 * M + 3) * SM::SV + s] = Xin[S3_P<M>() * N + g];
-        }
-        // ---- conserved words of the output cells ----
-        for (int t = threadIdx.x; t < ex * ey * ez; t += NT3) {
-            const int x = t % ex, y = (t / ex) % ey, z = t / (ex * ey);
-            const long long g = off + (i0 + x) + (long long)nx * ((j0 + y) + (long long)ny * (k0 + z));
-            const int c = x + TX * (y + TY * z);
-#pragma unroll
-            for (int m = 0; m < M; ++m) {
-                sm[SM::C_OFF + m * SM::CV + c] = Xin[S3_A<M>(m) * N + g];
-                sm[SM::C_OFF + (M + m) * SM::CV + c] = Xin[S3_AR<M>(m) * N + g];
-            }
-#pragma unroll
-            for (int r = 0; r < 3; ++r) sm[SM::C_OFF + (2 * M + r) * SM::CV + c] = Xin[S3_RU<M>(r) * N + g];
-            sm[SM::C_OFF + (2 * M + 3) * SM::CV + c] = Xin[S3_EH<M>() * N + g];
-            sm[SM::C_OFF + (2 * M + 4) * SM::CV + c] = Xin[S3_EL<M>() * N + g];
-        }
-        __syncthreads();
 
 #pragma unroll 1
         for (int d = 0; d < 3; ++d) {
@@ -366,10 +437,10 @@ __global__ void __launch_bounds__(NT3) k_stage3d(M3P P, M3B b, int stage, int fo
                 const int sR = (x + 2) + SM::SX * ((y + 2) + SM::SY * (z + 2));
                 const int sL = sR - stride;
                 FS3<M> L, R;
-                if (posR == 0) recon3<M, TX, TY, TZ>(P, sm, sR, stride, 1, d, lo_refl, L);  // image of UR(0)
-                else recon3<M, TX, TY, TZ>(P, sm, sL, stride, 1, d, false, L);
-                if (posR == n_d) recon3<M, TX, TY, TZ>(P, sm, sL, stride, 0, d, hi_refl, R);  // image of UL(n-1)
-                else recon3<M, TX, TY, TZ>(P, sm, sR, stride, 0, d, false, R);
+                if (posR == 0) recon3<M, TX, TY, TZ>(P, sp, sR, stride, 1, d, lo_refl, L);  // image of UR(0)
+                else recon3<M, TX, TY, TZ>(P, sp, sL, stride, 1, d, false, L);
+                if (posR == n_d) recon3<M, TX, TY, TZ>(P, sp, sL, stride, 0, d, hi_refl, R);  // image of UL(n-1)
+                else recon3<M, TX, TY, TZ>(P, sp, sR, stride, 0, d, false, R);
                 float F[2 * M + 5];
                 hllc3<M>(L, R, d, F);
                 const int fidx = x + fx * (y + fy * z);
@@ -387,10 +458,10 @@ __global__ void __launch_bounds__(NT3) k_stage3d(M3P P, M3B b, int stage, int fo
                 const int s = (x + 2) + SM::SX * ((y + 2) + SM::SY * (z + 2));
                 const float* Fl = sm + SM::F_OFF;
                 const float dS = Fl[(2 * M + 4) * SM::FV + f0] - Fl[(2 * M + 4) * SM::FV + f1];
-                float* C = sm + SM::C_OFF;
+                float* C = sp + SM::C_OFF;
 #pragma unroll
                 for (int m = 0; m < M; ++m) {
-                    const float a0 = sm[SM::P_OFF + m * SM::SV + s];
+                    const float a0 = sp[SM::P_OFF + m * SM::SV + s];
                     C[m * SM::CV + c] += dtdx * (Fl[m * SM::FV + f0] - Fl[m * SM::FV + f1] - a0 * dS);
                     C[(M + m) * SM::CV + c] += dtdx * (Fl[(M + m) * SM::FV + f0] - Fl[(M + m) * SM::FV + f1]);
                 }
@@ -412,7 +483,7 @@ __global__ void __launch_bounds__(NT3) k_stage3d(M3P P, M3B b, int stage, int fo
             const int gi = i0 + x, gj = j0 + y, gk = k0 + z;
             const long long g = off + gi + (long long)nx * (gj + (long long)ny * gk);
             const int c = x + TX * (y + TY * z);
-            const float* C = sm + SM::C_OFF;
+            const float* C = sp + SM::C_OFF;
             float a[M], ar[M], rk[M], ru[3], u[3], eh, el, p;
 #pragma unroll
             for (int m = 0; m < M; ++m) {
