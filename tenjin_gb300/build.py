@@ -36,6 +36,16 @@ UNITS = {
     "tj_adjoint.cu": ["-fmad=false"],
 }
 
+# The per-direction kernels, one object per (type, material count, direction)
+# instance of tj_path_inst.cu; M = 0 / direction -1 is the generic instance.
+_INST = [(1, 0), (1, 1), (1, 2), (2, 0), (2, 1), (2, 2), (0, -1)]
+INSTANCES = {
+    f"tj_path_{r}_m{m}_d{'g' if d < 0 else d}.o":
+        ("tj_path_inst.cu", [f"-DTJ_INST_R={r}", f"-DTJ_INST_M={m}", f"-DTJ_INST_D={d}",
+                             "-fmad=false" if r == 64 else "-use_fast_math"])
+    for r in (64, 32) for m, d in _INST
+}
+
 
 def nvcc() -> str:
     for cand in (shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
@@ -52,23 +62,26 @@ def _deps_mtime() -> float:
     return t
 
 
-def _compile(unit: str, extra) -> str:
+def _compile(obj_name: str, unit: str, extra) -> str:
     src = os.path.join(CSRC, unit)
-    obj = os.path.join(BUILD, unit.replace(".cu", ".o"))
+    obj = os.path.join(BUILD, obj_name)
     cmd = [nvcc()] + ARCH + COMMON + extra + ["-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
-        raise RuntimeError(f"nvcc failed for {unit}:\n{r.stdout}\n{r.stderr}")
+        raise RuntimeError(f"nvcc failed for {obj_name}:\n{r.stdout}\n{r.stderr}")
     return obj
 
 
 def build(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
-    units = {u: f for u, f in UNITS.items() if os.path.exists(os.path.join(CSRC, u))}
+    jobs = [(u.replace(".cu", ".o"), u, f) for u, f in UNITS.items() if os.path.exists(os.path.join(CSRC, u))]
+    jobs += [(o, u, f) for o, (u, f) in INSTANCES.items()]
     if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= _deps_mtime():
         return LIB
-    with cf.ThreadPoolExecutor(max_workers=len(units)) as ex:
-        objs = list(ex.map(lambda kv: _compile(*kv), units.items()))
+    # the largest objects first, so that the parallel build ends together
+    jobs.sort(key=lambda j: (not j[0].startswith("tj_path_"), j[0]))
+    with cf.ThreadPoolExecutor(max_workers=min(len(jobs), max(2, os.cpu_count() or 2))) as ex:
+        objs = list(ex.map(lambda j: _compile(*j), jobs))
     cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

@@ -14,6 +14,7 @@
 
 #include "tj_mixed.cuh"
 #include "tj_path.cuh"
+#include "tj_path_launch.cuh"
 
 namespace tj {
 
@@ -152,25 +153,13 @@ struct General32 : MixedBase {
     {
         sync_geometry(fb);
         k_reset_dtmin32<<<1, 32, 0, st>>>(fb.scal);
-        k_cfl<<<nb32(b.ntot), kT32, 0, st>>>(P, b, (const float*)A);
-        return 2;
+        return 1 + path_cfl_any(P, b, (const float*)A, st, nullptr);
     }
 
     int stage(const float* X, float* Y, int finish, cudaStream_t st, Prof* pr)
     {
         int n = 0;
-        for (int d = 0; d < P.dim; ++d) {
-            if (pr) pr->begin("tj_recon_fp32", st);
-            k_recon<<<nb32(b.ntot), kT32, 0, st>>>(P, b, X, d);
-            if (pr) pr->end("tj_recon_fp32", st);
-            if (pr) pr->begin("tj_flux_fp32", st);
-            k_flux<<<nb32(b.nftot[d]), kT32, 0, st>>>(P, b, d);
-            if (pr) pr->end("tj_flux_fp32", st);
-            if (pr) pr->begin("tj_update_fp32", st);
-            k_update<<<nb32(b.ntot), kT32, 0, st>>>(P, b, X, Y, d, d == 0, d == P.dim - 1, finish);
-            if (pr) pr->end("tj_update_fp32", st);
-            n += 3;
-        }
+        for (int d = 0; d < P.dim; ++d) n += path_dir_any(P, b, X, Y, d, d == 0, d == P.dim - 1, finish, st, pr);
         return n;
     }
 
@@ -178,10 +167,7 @@ struct General32 : MixedBase {
     {
         sync_geometry(fb);
         int n = 0;
-        if (pr) pr->begin("tj_cfl_fp32", st);
-        k_cfl<<<nb32(b.ntot), kT32, 0, st>>>(P, b, (const float*)A);
-        if (pr) pr->end("tj_cfl_fp32", st);
-        n += 1;
+        n += path_cfl_any(P, b, (const float*)A, st, pr);
         n += fp64_dt_finalize(DP, fb, 1, st);
         n += stage(A, B, 0, st, pr);
         n += stage(B, C, 1, st, pr);

@@ -18,6 +18,7 @@
 #include <cuda_runtime.h>
 
 #include "tj_path.cuh"
+#include "tj_path_launch.cuh"
 
 namespace tj {
 
@@ -264,10 +265,7 @@ __global__ void k_prim_to_state(DevParams P, Fp64Bufs b, int dom, const double* 
 
 int fp64_cfl(const DevParams& P, const Fp64Bufs& b, const double* X, cudaStream_t st, Prof* pr)
 {
-    PROF_BEGIN("tj_cfl_fp64");
-    k_cfl<<<nblocks(b.ntot), kThreads, 0, st>>>(P, b, X);
-    PROF_END("tj_cfl_fp64");
-    return 1;
+    return path_cfl_any(P, b, X, st, pr);
 }
 
 int fp64_dt_finalize(const DevParams& P, const Fp64Bufs& b, int clamp, cudaStream_t st)
@@ -279,18 +277,7 @@ int fp64_dt_finalize(const DevParams& P, const Fp64Bufs& b, int clamp, cudaStrea
 int fp64_stage(const DevParams& P, const Fp64Bufs& b, const double* X, double* Y, int finish, cudaStream_t st, Prof* pr)
 {
     int n = 0;
-    for (int d = 0; d < P.dim; ++d) {
-        PROF_BEGIN("tj_recon_fp64");
-        k_recon<<<nblocks(b.ntot), kThreads, 0, st>>>(P, b, X, d);
-        PROF_END("tj_recon_fp64");
-        PROF_BEGIN("tj_flux_fp64");
-        k_flux<<<nblocks(b.nftot[d]), kThreads, 0, st>>>(P, b, d);
-        PROF_END("tj_flux_fp64");
-        PROF_BEGIN("tj_update_fp64");
-        k_update<<<nblocks(b.ntot), kThreads, 0, st>>>(P, b, X, Y, d, d == 0, d == P.dim - 1, finish);
-        PROF_END("tj_update_fp64");
-        n += 3;
-    }
+    for (int d = 0; d < P.dim; ++d) n += path_dir_any(P, b, X, Y, d, d == 0, d == P.dim - 1, finish, st, pr);
     return n;
 }
 

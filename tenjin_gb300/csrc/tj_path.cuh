@@ -341,9 +341,12 @@ __device__ inline void thinc_cand(const PT& P, const DevDomain& D, const R* X, l
 // ---------------------------------------------------------------------------
 // Reconstruction of one direction.
 // ---------------------------------------------------------------------------
-template <typename PT, typename R = typename PT::real>
-__global__ void k_recon(PT P, PathBufs<typename PT::real> b, const R* __restrict__ X, int d)
+// DC >= 0: the direction as a compile-time constant (d is then ignored).
+template <typename PT, int DC = -1, typename R = typename PT::real>
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1)
+    k_recon(PT P, PathBufs<typename PT::real> b, const R* __restrict__ X, int dyn_d)
 {
+    const int d = DC >= 0 ? DC : dyn_d;
     if (b.scal->done) return;
     const long long nt = b.ntot;
     for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < nt; g += (long long)gridDim.x * blockDim.x) {
@@ -446,6 +449,7 @@ __global__ void k_recon(PT P, PathBufs<typename PT::real> b, const R* __restrict
         }
         // cleanUpAlpha of UL and UR: nbox-b times for box b, the closures see
         // the first (hllc.cpp:628-638).
+#pragma unroll
         for (int side = 0; side < 2; ++side) {
             CellT<R>& S = side ? Rc : L;
             if (reps > 0) {
@@ -501,96 +505,163 @@ __device__ inline void star_state(const PT& P, const CellT<R>& U, CellT<R>& Us, 
     Us.E = mult * U.rho * (U.E / U.rho + (Ss - ud) * (Ss - (U.sigma[4 * d]) / (U.rho * (SK - ud))));
 }
 
-// Physical flux of the conservative variables (flux.cpp:33-47) into the
-// flux-word layout.
+// The conservative variables of one state, or their fluxes, by name: kept in
+// registers; the flux-word layout is applied only where a face is stored.
+template <typename R>
+struct FluxV {
+    R alpha[TJ_MAX_MAT], arho[TJ_MAX_MAT], rhou[3], E, V[9], are[TJ_MAX_MAT], arl;
+};
+
+// Physical flux of the conservative variables (flux.cpp:33-47).
 template <typename PT, typename R = typename PT::real>
-__device__ inline void phys_flux(const PT& P, const CellT<R>& U, int d, R* F)
+__device__ inline void phys_flux(const PT& P, const CellT<R>& U, int d, FluxV<R>& F)
 {
     R ud = U.vel[d];
     for (int m = 0; m < P.M; ++m) {
-        F[P.X_ALPHA + m] = U.alpha[m] * ud;
-        F[P.X_ARHO + m] = U.arho[m] * ud;
+        F.alpha[m] = U.alpha[m] * ud;
+        F.arho[m] = U.arho[m] * ud;
     }
 #pragma unroll
-    for (int r = 0; r < 3; ++r) F[P.X_RHOU + r] = U.rhou[r] * ud - U.sigma[3 * r + d];
+    for (int r = 0; r < 3; ++r) F.rhou[r] = U.rhou[r] * ud - U.sigma[3 * r + d];
     R vs = R(0.0);
 #pragma unroll
     for (int i = 0; i < 3; ++i) vs += U.vel[i] * U.sigma[3 * i + d];
-    F[P.X_E] = U.E * ud - vs;
+    F.E = U.E * ud - vs;
     if (P.solid)
 #pragma unroll
         for (int q = 0; q < 9; ++q) {
             int row = q / 3, col = q % 3;
-            F[P.X_V + q] = U.V[q] * ud - U.V[3 * d + col] * U.vel[row];
+            F.V[q] = U.V[q] * ud - U.V[3 * d + col] * U.vel[row];
         }
     if (P.plastic)
-        for (int m = 0; m < P.M; ++m) F[P.X_ARE + m] = U.are[m] * ud;
-    if (P.nmix) F[P.X_ARL] = U.arl * ud;
+        for (int m = 0; m < P.M; ++m) F.are[m] = U.are[m] * ud;
+    if (P.nmix) F.arl = U.arl * ud;
 }
 
-// Conservative values of a state in the flux-word layout.
+// Conservative values of a state.
 template <typename PT, typename R = typename PT::real>
-__device__ inline void cons_vals(const PT& P, const CellT<R>& U, R* Q)
+__device__ inline void cons_vals(const PT& P, const CellT<R>& U, FluxV<R>& Q)
 {
     for (int m = 0; m < P.M; ++m) {
-        Q[P.X_ALPHA + m] = U.alpha[m];
-        Q[P.X_ARHO + m] = U.arho[m];
+        Q.alpha[m] = U.alpha[m];
+        Q.arho[m] = U.arho[m];
     }
 #pragma unroll
-    for (int r = 0; r < 3; ++r) Q[P.X_RHOU + r] = U.rhou[r];
-    Q[P.X_E] = U.E;
+    for (int r = 0; r < 3; ++r) Q.rhou[r] = U.rhou[r];
+    Q.E = U.E;
     if (P.solid)
 #pragma unroll
-        for (int q = 0; q < 9; ++q) Q[P.X_V + q] = U.V[q];
+        for (int q = 0; q < 9; ++q) Q.V[q] = U.V[q];
     if (P.plastic)
-        for (int m = 0; m < P.M; ++m) Q[P.X_ARE + m] = U.are[m];
-    if (P.nmix) Q[P.X_ARL] = U.arl;
+        for (int m = 0; m < P.M; ++m) Q.are[m] = U.are[m];
+    if (P.nmix) Q.arl = U.arl;
 }
 
-#define TJ_MAXX 32
+// The face flux of every conservative variable but alpha, in the reference's
+// evaluation order (hllc.cpp:416-476, 287-371):
+//   NT = 0: FK
+//   NT = 1: FK + S1 (Q1 - Q0)
+//   NT = 2: FK + S1 (Q1 - Q0) + S2 (Q2 - Q1)
+// alpha takes the flux of the star state FA.
+template <int NT, typename PT, typename R = typename PT::real>
+__device__ inline void flux_combine(const PT& P, FluxV<R>& F, const FluxV<R>& FA, const FluxV<R>& FK,
+                                    const FluxV<R>& Q0, const FluxV<R>& Q1, const FluxV<R>& Q2, R S1, R S2)
+{
+    auto one = [&](R fk, R q0, R q1, R q2) -> R {
+        if constexpr (NT == 0) return fk;
+        else if constexpr (NT == 1) return fk + S1 * (q1 - q0);
+        else return fk + S1 * (q1 - q0) + S2 * (q2 - q1);
+    };
+    for (int m = 0; m < P.M; ++m) {
+        F.alpha[m] = FA.alpha[m];
+        F.arho[m] = one(FK.arho[m], Q0.arho[m], Q1.arho[m], Q2.arho[m]);
+    }
+#pragma unroll
+    for (int r = 0; r < 3; ++r) F.rhou[r] = one(FK.rhou[r], Q0.rhou[r], Q1.rhou[r], Q2.rhou[r]);
+    F.E = one(FK.E, Q0.E, Q1.E, Q2.E);
+    if (P.solid)
+#pragma unroll
+        for (int q = 0; q < 9; ++q) F.V[q] = one(FK.V[q], Q0.V[q], Q1.V[q], Q2.V[q]);
+    if (P.plastic)
+        for (int m = 0; m < P.M; ++m) F.are[m] = one(FK.are[m], Q0.are[m], Q1.are[m], Q2.are[m]);
+    if (P.nmix) F.arl = one(FK.arl, Q0.arl, Q1.arl, Q2.arl);
+}
 
-// Returns the side whose star alpha the face carries: 0 left, 1 right.
+// One face into the flux-word layout (nf faces per word).
 template <typename PT, typename R = typename PT::real>
-__device__ inline int face_flux(const PT& P, const CellT<R>& L, const CellT<R>& Rc, int d, R* F, DevScalars* scal)
+__device__ inline void store_flux(const PT& P, R* FX, long long nf, long long f, const FluxV<R>& F, R Ss,
+                                  const R* vstar)
+{
+#define FXS(w) FX[(long long)(w) * nf + f]
+    for (int m = 0; m < P.M; ++m) {
+        FXS(P.X_ALPHA + m) = F.alpha[m];
+        FXS(P.X_ARHO + m) = F.arho[m];
+    }
+#pragma unroll
+    for (int r = 0; r < 3; ++r) FXS(P.X_RHOU + r) = F.rhou[r];
+    FXS(P.X_E) = F.E;
+    if (P.solid) {
+#pragma unroll
+        for (int q = 0; q < 9; ++q) FXS(P.X_V + q) = F.V[q];
+#pragma unroll
+        for (int col = 0; col < 3; ++col) FXS(P.X_VSTAR + col) = vstar[col];
+    }
+    if (P.plastic)
+        for (int m = 0; m < P.M; ++m) FXS(P.X_ARE + m) = F.are[m];
+    if (P.nmix) FXS(P.X_ARL) = F.arl;
+    FXS(P.X_SSTAR) = Ss;
+#undef FXS
+}
+
+// HLLC (hllc.cpp:384-487) or the 5-wave solver (133-380) at one face. F gets
+// the conservative fluxes, Ss the contact speed, vstar the VSTAR(d, col)
+// values (solids). Returns the side whose star alpha the face carries: 0
+// left, 1 right.
+template <typename PT, typename R = typename PT::real>
+__device__ inline int face_flux(const PT& P, const CellT<R>& L, const CellT<R>& Rc, int d, FluxV<R>& F, R& Ss,
+                                R* vstar, DevScalars* scal)
 {
     R x1 = fabs(L.vel[d]) + L.a, x2 = fabs(Rc.vel[d]) + Rc.a;
     R SR = (x1 < x2) ? x2 : x1;
     R SL = -SR;
-    R Ss = (-Rc.sigma[4 * d] + L.sigma[4 * d] + L.rhou[d] * (SL - L.vel[d]) - Rc.rhou[d] * (SR - Rc.vel[d])) /
-                (L.rho * (SL - L.vel[d]) - Rc.rho * (SR - Rc.vel[d]));  // getSstar, hllc.cpp:5-8
-    F[P.X_SSTAR] = Ss;
-    const int nx = P.X_SSTAR;  // words before S*: the conservative variables
-    R FK[TJ_MAXX], QK[TJ_MAXX], QS[TJ_MAXX], FS[TJ_MAXX];
-    CellT<R> Ls, Rs;
+    Ss = (-Rc.sigma[4 * d] + L.sigma[4 * d] + L.rhou[d] * (SL - L.vel[d]) - Rc.rhou[d] * (SR - Rc.vel[d])) /
+         (L.rho * (SL - L.vel[d]) - Rc.rho * (SR - Rc.vel[d]));  // getSstar, hllc.cpp:5-8
     if (!P.solid) {
-        int side;
-        const CellT<R>* K;
-        R SK;
-        bool hllc;
-        if (SL >= R(0.0)) { side = 0; K = &L; SK = SL; hllc = false; }
-        else if (Ss >= R(0.0)) { side = 0; K = &L; SK = SL; hllc = true; }
-        else if (SR >= R(0.0)) { side = 1; K = &Rc; SK = SR; hllc = true; }
-        else { side = 1; K = &Rc; SK = SR; hllc = false; }
-        CellT<R>& Ks = side ? Rs : Ls;
-        star_state(P, *K, Ks, SK, Ss, d);
-        phys_flux(P, *K, d, FK);
-        phys_flux(P, Ks, d, FS);
-        cons_vals(P, *K, QK);
-        cons_vals(P, Ks, QS);
-        for (int w = 0; w < nx; ++w) {
-            bool is_alpha = w < P.X_ALPHA + P.M;
-            F[w] = is_alpha ? FS[w] : (hllc ? FK[w] + SK * (QS[w] - QK[w]) : FK[w]);
+        // the state K of the upwind side and its star state (no pointer or
+        // reference selects between L and Rc: both stay in registers)
+        auto hllc_side = [&](const CellT<R>& K, R SK, bool hllc) {
+            CellT<R> Ks;
+            star_state(P, K, Ks, SK, Ss, d);
+            FluxV<R> FK, FS, QK, QS;
+            phys_flux(P, K, d, FK);
+            phys_flux(P, Ks, d, FS);
+            if (hllc) {
+                cons_vals(P, K, QK);
+                cons_vals(P, Ks, QS);
+                flux_combine<1>(P, F, FS, FK, QK, QS, QS, SK, R(0.0));
+            } else {
+                flux_combine<0>(P, F, FS, FK, FK, FK, FK, R(0.0), R(0.0));
+            }
+        };
+        if (SL >= R(0.0) || Ss >= R(0.0)) {
+            hllc_side(L, SL, !(SL >= R(0.0)));
+            return 0;
         }
-        return side;
+        hllc_side(Rc, SR, SR >= R(0.0));
+        return 1;
     }
+    CellT<R> Ls, Rs;
 
     // 5-wave solver for solids (hllc.cpp:133-380).
     if (isnan(SL) || isnan(SR) || isnan(Ss)) { set_status(scal, TJ_ERR_WAVESPEED); return 0; }
     R SLT = R(0.0), SRT = R(0.0);
     CellT<R> Uss;
-    R QL[TJ_MAXX], QR[TJ_MAXX], QLs[TJ_MAXX], QRs[TJ_MAXX], QSS[TJ_MAXX], FL[TJ_MAXX], FR[TJ_MAXX], FAs[TJ_MAXX];
-    const R* vsrc;
+    FluxV<R> QK, QKs, QSS, FK, FAs;
     int side;
+    auto vstar_of = [&](const CellT<R>& U) {  // VSTAR(d, col), read by update
+#pragma unroll
+        for (int col = 0; col < 3; ++col) vstar[col] = U.V[3 * d + col];
+    };
     auto starstar = [&](const CellT<R>& UK, CellT<R>& UKs, R SKT) {  // getStarStarState, hllc.cpp:87-129
         Uss = UKs;
 #pragma unroll
@@ -614,68 +685,67 @@ __device__ inline int face_flux(const PT& P, const CellT<R>& L, const CellT<R>& 
                 Uss.V[3 * row + col] += (Uss.V[3 * d + col] * (Uss.vel[row] - UK.vel[row])) / (Ss - SKT);
         }
     };
-    phys_flux(P, L, d, FL);
-    phys_flux(P, Rc, d, FR);
-    cons_vals(P, L, QL);
-    cons_vals(P, Rc, QR);
     if (SL >= R(0.0)) {
         star_state(P, L, Ls, SL, Ss, d);
         phys_flux(P, Ls, d, FAs);
-        for (int w = 0; w < nx; ++w) F[w] = (w < P.X_ALPHA + P.M) ? FAs[w] : FL[w];
-        vsrc = L.V;
+        phys_flux(P, L, d, FK);
+        flux_combine<0>(P, F, FAs, FK, FK, FK, FK, R(0.0), R(0.0));
+        vstar_of(L);
         side = 0;
     } else if (Ss >= R(0.0)) {
         star_state(P, L, Ls, SL, Ss, d);
         SLT = Ss - transverse_speed(P, Ls);
         phys_flux(P, Ls, d, FAs);
-        cons_vals(P, Ls, QLs);
+        phys_flux(P, L, d, FK);
+        cons_vals(P, L, QK);
+        cons_vals(P, Ls, QKs);
         if (SLT >= R(0.0)) {
-            for (int w = 0; w < nx; ++w) F[w] = (w < P.X_ALPHA + P.M) ? FAs[w] : FL[w] + SL * (QLs[w] - QL[w]);
-            vsrc = Ls.V;
+            flux_combine<1>(P, F, FAs, FK, QK, QKs, QKs, SL, R(0.0));
+            vstar_of(Ls);
         } else {
             star_state(P, Rc, Rs, SR, Ss, d);
             SRT = Ss + transverse_speed(P, Rs);
             starstar(L, Ls, SLT);
             cons_vals(P, Uss, QSS);
-            for (int w = 0; w < nx; ++w)
-                F[w] = (w < P.X_ALPHA + P.M) ? FAs[w] : FL[w] + SL * (QLs[w] - QL[w]) + SLT * (QSS[w] - QLs[w]);
-            vsrc = Uss.V;
+            flux_combine<2>(P, F, FAs, FK, QK, QKs, QSS, SL, SLT);
+            vstar_of(Uss);
         }
         side = 0;
     } else if (SR >= R(0.0)) {
         star_state(P, Rc, Rs, SR, Ss, d);
         SRT = Ss + transverse_speed(P, Rs);
         phys_flux(P, Rs, d, FAs);
-        cons_vals(P, Rs, QRs);
+        phys_flux(P, Rc, d, FK);
+        cons_vals(P, Rc, QK);
+        cons_vals(P, Rs, QKs);
         if (SRT >= R(0.0)) {
             star_state(P, L, Ls, SL, Ss, d);
             SLT = Ss - transverse_speed(P, Ls);
             starstar(Rc, Rs, SRT);
             cons_vals(P, Uss, QSS);
-            for (int w = 0; w < nx; ++w)
-                F[w] = (w < P.X_ALPHA + P.M) ? FAs[w] : FR[w] + SR * (QRs[w] - QR[w]) + SRT * (QSS[w] - QRs[w]);
-            vsrc = Uss.V;
+            flux_combine<2>(P, F, FAs, FK, QK, QKs, QSS, SR, SRT);
+            vstar_of(Uss);
         } else {
-            for (int w = 0; w < nx; ++w) F[w] = (w < P.X_ALPHA + P.M) ? FAs[w] : FR[w] + SR * (QRs[w] - QR[w]);
-            vsrc = Rs.V;
+            flux_combine<1>(P, F, FAs, FK, QK, QKs, QKs, SR, R(0.0));
+            vstar_of(Rs);
         }
         side = 1;
     } else {
         star_state(P, Rc, Rs, SR, Ss, d);
         phys_flux(P, Rs, d, FAs);
-        for (int w = 0; w < nx; ++w) F[w] = (w < P.X_ALPHA + P.M) ? FAs[w] : FR[w];
-        vsrc = Rc.V;
+        phys_flux(P, Rc, d, FK);
+        flux_combine<0>(P, F, FAs, FK, FK, FK, FK, R(0.0), R(0.0));
+        vstar_of(Rc);
         side = 1;
     }
-#pragma unroll
-    for (int col = 0; col < 3; ++col) F[P.X_VSTAR + col] = vsrc[3 * d + col];  // VSTAR(d, col), read by update
     if (isnan(SL) || isnan(SR) || isnan(Ss) || isnan(SLT) || isnan(SRT)) set_status(scal, TJ_ERR_WAVESPEED);
     return side;
 }
 
-template <typename PT, typename R = typename PT::real>
-__global__ void k_flux(PT P, PathBufs<typename PT::real> b, int d)
+template <typename PT, int DC = -1, typename R = typename PT::real>
+__global__ void k_flux(PT P, PathBufs<typename PT::real> b, int dyn_d)
 {
+    const int d = DC >= 0 ? DC : dyn_d;
     if (b.scal->done) return;
     const long long nt = b.ntot, nf = b.nftot[d];
     for (long long f = blockIdx.x * (long long)blockDim.x + threadIdx.x; f < nf; f += (long long)gridDim.x * blockDim.x) {
@@ -693,9 +763,10 @@ __global__ void k_flux(PT P, PathBufs<typename PT::real> b, int d)
         CellT<R> L, Rc;
         load_face(P, b.UR, nt, gl, rl[d] ? d : -1, L);
         load_face(P, b.UL, nt, gr, rr[d] ? d : -1, Rc);
-        R F[TJ_MAXX];
-        int side = face_flux(P, L, Rc, d, F, b.scal);
-        for (int w = 0; w < P.NX; ++w) b.FX[(long long)w * nf + f] = F[w];
+        FluxV<R> F;
+        R Ss, vstar[3] = {R(0.0), R(0.0), R(0.0)};
+        int side = face_flux(P, L, Rc, d, F, Ss, vstar, b.scal);
+        store_flux(P, b.FX, nf, f, F, Ss, vstar);
         if (P.thinc) {
             const CellT<R>& src = side ? Rc : L;
             int idx[3] = {i, j, k};
@@ -927,10 +998,12 @@ __device__ inline void radial_source(const PT& P, CellT<R>& c, const R* sg, int 
 // Update of one direction; last direction: c2p; second stage: average and
 // the post-advance operators of main.cpp:145-187.
 // ---------------------------------------------------------------------------
-template <typename PT, typename R = typename PT::real>
-__global__ void k_update(PT P, PathBufs<typename PT::real> b, const R* __restrict__ X, R* Y, int d, int first, int last,
-                         int finish)
+template <typename PT, int DC = -1, typename R = typename PT::real>
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1)
+    k_update(PT P, PathBufs<typename PT::real> b, const R* __restrict__ X, R* Y, int dyn_d, int first, int last,
+             int finish)
 {
+    const int d = DC >= 0 ? DC : dyn_d;
     if (b.scal->done) return;
     const long long nt = b.ntot, nf = b.nftot[d];
     const R dtdx_num = b.scal->dt;

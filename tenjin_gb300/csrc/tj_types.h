@@ -61,6 +61,16 @@ struct DevParams32 {
     DevParams d;
 };
 
+// A parameter block whose material count is a compile-time constant: the
+// static member M hides the base's runtime M, so that the per-material loops
+// of the kernels unroll and their per-material arrays stay in registers.
+template <class Base, int MC>
+struct WithM : Base {
+    static constexpr int M = MC;
+    WithM() = default;
+    explicit WithM(const Base& b) : Base(b) {}
+};
+
 // One independent domain: valid cells [0,n) per axis, stored contiguously
 // from cell offset `off` (i fastest) in every state block.
 struct DevDomain {
