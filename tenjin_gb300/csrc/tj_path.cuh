@@ -743,7 +743,7 @@ __device__ inline int face_flux(const PT& P, const CellT<R>& L, const CellT<R>& 
 }
 
 template <typename PT, int DC = -1, typename R = typename PT::real>
-__global__ void k_flux(PT P, PathBufs<typename PT::real> b, int dyn_d)
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1) k_flux(PT P, PathBufs<typename PT::real> b, int dyn_d)
 {
     const int d = DC >= 0 ? DC : dyn_d;
     if (b.scal->done) return;
@@ -861,7 +861,8 @@ template <typename PT, typename R = typename PT::real>
 __device__ inline int plastic_cell_in64(const PT& P, CellT<R>& c)
 {
     CellT<double> d;
-    for (int m = 0; m < TJ_MAX_MAT; ++m) {
+    const DevParams& PD = P.d;
+    for (int m = 0; m < P.M; ++m) {
         d.alpha[m] = c.alpha[m];
         d.arho[m] = c.arho[m];
         d.rhok[m] = c.rhok[m];
@@ -885,9 +886,9 @@ __device__ inline int plastic_cell_in64(const PT& P, CellT<R>& c)
         d.V[q] = c.V[q];
         d.devH[q] = c.devH[q];
     }
-    const int e = plastic_cell(P.d, d);
-    c2p(P.d, d);
-    for (int m = 0; m < TJ_MAX_MAT; ++m) {
+    const int e = plastic_cell(PD, d);
+    c2p(PD, d);
+    for (int m = 0; m < P.M; ++m) {
         c.alpha[m] = (R)d.alpha[m];
         c.arho[m] = (R)d.arho[m];
         c.rhok[m] = (R)d.rhok[m];
