@@ -236,9 +236,13 @@ def run_gpu_arm(args):
         torch.cuda.synchronize()
         e2e_ms = e0.elapsed_time(e1)
         wall = time.perf_counter() - t0
-        nbytes = nc * ncell * 8
+        from tenjin_gb300.host import carried_components
+        # the upload copies the component planes of the carried state, the
+        # download all Ncomp components of the AccessPattern
+        up_bytes = len(carried_components(case)) * ncell * 8
+        down_bytes = nc * ncell * 8
         e2e = {"value": ncell * args.e2e_steps / (max(e2e_ms / 1e3, wall)), "unit": "cell-updates/s",
-               "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes, "steps": args.e2e_steps,
+               "h2d_bytes_per_step": up_bytes, "d2h_bytes_per_step": down_bytes, "steps": args.e2e_steps,
                "path": "tj_upload_domain + tj_step + tj_download_domain (AccessPattern layout, pinned host)"}
 
     # accuracy and the FP64 speeds: the whole 2000-step workload (not part of

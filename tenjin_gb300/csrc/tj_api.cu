@@ -629,13 +629,29 @@ static int exchange(tj_ctx* c, int q, const int* bx, double* host, int ncomp, in
     e = ensure_staging(c, bytes);
     if (e) return e;
     Fp64Bufs b = bufs(c);
-    a_sync(c);  // the cells outside this box keep their current values
     if (up) {
-        TJ_CUDA(c, cudaMemcpyAsync(c->staging, host, bytes, cudaMemcpyDefault, c->stream));
+        // the cells outside this box keep their current values; a box that is
+        // the whole of the only domain replaces the state entirely
+        const DevDomain& Dq = c->doms[q];
+        const bool whole = c->doms.size() == 1 && bx[0] == 0 && bx[1] == 0 && bx[2] == 0 && bx[3] == Dq.n[0] - 1 &&
+                           bx[4] == Dq.n[1] - 1 && bx[5] == Dq.n[2] - 1;
+        if (!whole) a_sync(c);
+        // only the component planes the carried state is built from cross the
+        // link (k_ap_to_state reads no other)
+        const DevParams& P = c->P;
+        int rng[5][2] = {{P.A_ALPHA, P.A_P + 1}, {-1, -1}, {-1, -1}, {-1, -1}, {-1, -1}};
+        if (P.nmix) { rng[1][0] = P.A_RMIX; rng[1][1] = P.A_ARL + 1; }
+        if (P.solid) { rng[2][0] = P.A_V; rng[2][1] = P.A_V + 9; rng[3][0] = P.A_HJ2; rng[3][1] = P.A_HJ2 + 1; }
+        if (P.plastic) { rng[4][0] = P.A_EPS; rng[4][1] = P.A_ARE + P.M; }
+        for (auto& r : rng)
+            if (r[0] >= 0)
+                TJ_CUDA(c, cudaMemcpyAsync(c->staging + (size_t)r[0] * cs, host + (size_t)r[0] * cs,
+                                           sizeof(double) * (size_t)(r[1] - r[0]) * cs, cudaMemcpyDefault, c->stream));
         c->launches += fp64_ap_to_state(c->P, b, q, bx, c->staging, ld_i, ld_j, ld_k, cs, ngrow, c->A, c->stream);
         a_written(c);
         TJ_CUDA(c, cudaStreamSynchronize(c->stream));
     } else {
+        a_sync(c);
         if (ngrow > 0) TJ_CUDA(c, cudaMemcpyAsync(c->staging, host, bytes, cudaMemcpyDefault, c->stream));
         c->launches += fp64_state_to_ap(c->P, b, q, bx, c->A, c->staging, ld_i, ld_j, ld_k, cs, ngrow, c->stream);
         TJ_CUDA(c, cudaMemcpyAsync(host, c->staging, bytes, cudaMemcpyDefault, c->stream));
