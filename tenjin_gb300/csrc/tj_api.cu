@@ -117,6 +117,11 @@ struct tj_ctx {
     double *ulstar = nullptr, *urstar = nullptr, *gstar[3] = {nullptr, nullptr, nullptr};
     double* staging = nullptr;
     size_t staging_bytes = 0;
+    // whole-box downloads: the copy of each converted slab runs on a second
+    // stream while the next slab is converted
+    static constexpr int kSlabs = 8;
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t slab_ev[kSlabs + 1] = {};
     MixedState mixed;
     // graph-captured step groups
     cudaGraphExec_t graph_exec = nullptr;
@@ -479,6 +484,9 @@ int tj_destroy(tj_ctx* c)
     delete c->prof;
     c->prof = nullptr;
     if (c->d_scal) cudaFree(c->d_scal);
+    for (cudaEvent_t& e : c->slab_ev)
+        if (e) cudaEventDestroy(e);
+    if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return TJ_OK;
@@ -652,9 +660,30 @@ static int exchange(tj_ctx* c, int q, const int* bx, double* host, int ncomp, in
         TJ_CUDA(c, cudaStreamSynchronize(c->stream));
     } else {
         a_sync(c);
-        if (ngrow > 0) TJ_CUDA(c, cudaMemcpyAsync(c->staging, host, bytes, cudaMemcpyDefault, c->stream));
-        c->launches += fp64_state_to_ap(c->P, b, q, bx, c->A, c->staging, ld_i, ld_j, ld_k, cs, ngrow, c->stream);
-        TJ_CUDA(c, cudaMemcpyAsync(host, c->staging, bytes, cudaMemcpyDefault, c->stream));
+        if (ngrow == 0 && cs >= (1 << 16)) {
+            // slab k's components are rows [t0, t1) of every plane: one 2-D copy
+            // per slab, overlapped with the conversion of slab k + 1
+            if (!c->copy_stream) {
+                TJ_CUDA(c, cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+                for (cudaEvent_t& e : c->slab_ev) TJ_CUDA(c, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+            }
+            const int K = tj_ctx::kSlabs;
+            for (int k = 0; k < K; ++k) {
+                const long long t0 = cs * k / K, t1 = cs * (k + 1) / K;
+                c->launches += fp64_state_to_ap(c->P, b, q, bx, c->A, c->staging, ld_i, ld_j, ld_k, cs, 0, c->stream, t0, t1);
+                TJ_CUDA(c, cudaEventRecord(c->slab_ev[k], c->stream));
+                TJ_CUDA(c, cudaStreamWaitEvent(c->copy_stream, c->slab_ev[k], 0));
+                TJ_CUDA(c, cudaMemcpy2DAsync(host + t0, sizeof(double) * (size_t)cs, c->staging + t0,
+                                             sizeof(double) * (size_t)cs, sizeof(double) * (size_t)(t1 - t0), ncomp,
+                                             cudaMemcpyDefault, c->copy_stream));
+            }
+            TJ_CUDA(c, cudaEventRecord(c->slab_ev[K], c->copy_stream));
+            TJ_CUDA(c, cudaStreamWaitEvent(c->stream, c->slab_ev[K], 0));
+        } else {
+            if (ngrow > 0) TJ_CUDA(c, cudaMemcpyAsync(c->staging, host, bytes, cudaMemcpyDefault, c->stream));
+            c->launches += fp64_state_to_ap(c->P, b, q, bx, c->A, c->staging, ld_i, ld_j, ld_k, cs, ngrow, c->stream);
+            TJ_CUDA(c, cudaMemcpyAsync(host, c->staging, bytes, cudaMemcpyDefault, c->stream));
+        }
         TJ_CUDA(c, cudaStreamSynchronize(c->stream));
     }
     TJ_CUDA(c, cudaGetLastError());

@@ -172,11 +172,12 @@ __global__ void k_ap_to_state(DevParams P, Fp64Bufs b, int dom, int lx, int ly, 
 }
 
 __global__ void k_state_to_ap(DevParams P, Fp64Bufs b, int dom, int lx, int ly, int lz, int nx, int ny, int nz,
-                              const double* X, double* ap, int ld_i, int ld_j, long long cs, int go)
+                              const double* X, double* ap, int ld_i, int ld_j, long long cs, int go, long long t0,
+                              long long t1)
 {
-    const long long nt = b.ntot, nb = (long long)nx * ny * nz;
+    const long long nt = b.ntot;
     const DevDomain D = b.doms[dom];
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nb; t += (long long)gridDim.x * blockDim.x) {
+    for (long long t = t0 + blockIdx.x * (long long)blockDim.x + threadIdx.x; t < t1; t += (long long)gridDim.x * blockDim.x) {
         int i = (int)(t % nx), j = (int)((t / nx) % ny), k = (int)(t / ((long long)nx * ny));
         long long dst = (i + go) + (long long)ld_i * ((j + (P.dim > 1 ? go : 0)) + (long long)ld_j * (k + (P.dim > 2 ? go : 0)));
         long long g = D.off + (lx + i) + (long long)D.n[0] * ((ly + j) + (long long)D.n[1] * (lz + k));
@@ -310,12 +311,14 @@ int fp64_ap_to_state(const DevParams& P, const Fp64Bufs& b, int dom, const int* 
 }
 
 int fp64_state_to_ap(const DevParams& P, const Fp64Bufs& b, int dom, const int* bx, const double* X, double* ap, int ld_i,
-                     int ld_j, int ld_k, long long cs, int go, cudaStream_t st)
+                     int ld_j, int ld_k, long long cs, int go, cudaStream_t st, long long t0, long long t1)
 {
     (void)ld_k;
     int nx = bx[3] - bx[0] + 1, ny = bx[4] - bx[1] + 1, nz = bx[5] - bx[2] + 1;
-    k_state_to_ap<<<nblocks((long long)nx * ny * nz), kThreads, 0, st>>>(P, b, dom, bx[0], bx[1], bx[2], nx, ny, nz, X, ap,
-                                                                         ld_i, ld_j, cs, go);
+    if (t1 < 0) t1 = (long long)nx * ny * nz;
+    if (t1 <= t0) return 0;
+    k_state_to_ap<<<nblocks(t1 - t0), kThreads, 0, st>>>(P, b, dom, bx[0], bx[1], bx[2], nx, ny, nz, X, ap, ld_i, ld_j,
+                                                         cs, go, t0, t1);
     return 1;
 }
 

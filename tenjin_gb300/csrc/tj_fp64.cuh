@@ -49,8 +49,10 @@ int fp64_cell_op(const DevParams& P, const Fp64Bufs& b, double* X, const double*
 // domain, ncomp x box cells, i fastest) <-> carried state.
 int fp64_ap_to_state(const DevParams& P, const Fp64Bufs& b, int dom, const int* box_lohi, const double* ap, int ld_i,
                      int ld_j, int ld_k, long long cstride, int ghost_off, double* X, cudaStream_t st);
+// Cells [t0, t1) of the box (box-linear index, i fastest); t1 < 0: all.
 int fp64_state_to_ap(const DevParams& P, const Fp64Bufs& b, int dom, const int* box_lohi, const double* X, double* ap,
-                     int ld_i, int ld_j, int ld_k, long long cstride, int ghost_off, cudaStream_t st);
+                     int ld_i, int ld_j, int ld_k, long long cstride, int ghost_off, cudaStream_t st,
+                     long long t0 = 0, long long t1 = -1);
 int fp64_prim_to_state(const DevParams& P, const Fp64Bufs& b, int dom, const double* prim, double* X, cudaStream_t st);
 
 }  // namespace tj
