@@ -329,13 +329,14 @@ struct Smem {
     static constexpr int C_OFF = U_OFF + NP * MS * MP;
     static constexpr int SAX_OFF = C_OFF + NC * CT;                      // star alpha of x faces, rows y0-1..y0+29
     static constexpr int CRX_OFF = SAX_OFF + (THINC ? M * 31 * CP : 0);  // x right candidates, rows y0-2..y0+28
-    static constexpr int MX_OFF = CRX_OFF + (THINC ? M * 31 * CP : 0);   // x mixed masks
-    static constexpr int SAY_OFF = MX_OFF + (THINC ? 31 * CP : 0);       // star alpha of y faces (output cells)
-    static constexpr int URV_OFF = SAY_OFF + (THINC ? M * CT : 0);       // new URStar values
-    static constexpr int URF_OFF = URV_OFF + (THINC ? M * CT : 0);       // new URStar masks
-    static constexpr int RED_OFF = URF_OFF + (THINC ? CT : 0);
+    static constexpr int RED_OFF = CRX_OFF + (THINC ? M * 31 * CP : 0);
     static constexpr int TOTAL = RED_OFF + 32;
-    static constexpr size_t BYTES = sizeof(R) * TOTAL;
+    // x mixed masks, one byte per cell (rows y0-2..y0+28), after the words
+    static constexpr int MXB = THINC ? 31 * CP : 0;
+    // 74.6 KB for binary32, M = 2, THINC: three CTAs fit on an SM; the star
+    // alpha of the y faces and the new URStar values go straight to global
+    // memory from the y sweep instead of through shared memory
+    static constexpr size_t BYTES = sizeof(R) * TOTAL + ((MXB + 15) / 16) * 16;
 };
 
 // The THINC candidate of the cell at staged position (tx, ty) along d.
@@ -432,7 +433,7 @@ __device__ void sweep_line(const MixP<R>& P, const MixB<R>& b, R* sm, int x0, in
                 else if (D == 0) trm = ur_read<R>(b, m, cell - 1, s);  // URStar before this sweep
                 else {
                     const int r = pos - 1 - (y0 - 2);
-                    const unsigned mx = (unsigned)sm[SM::MX_OFF + r * CP + (line - x0)];
+                    const unsigned mx = reinterpret_cast<const unsigned char*>(sm + SM::TOTAL)[r * CP + (line - x0)];
                     trm = ((mx >> m) & 1u) ? sm[SM::CRX_OFF + (m * 31 + r) * CP + (line - x0)]
                                            : ur_read<R>(b, m, cell - P.nx, s);
                 }
@@ -460,7 +461,7 @@ __device__ void sweep_line(const MixP<R>& P, const MixB<R>& b, R* sm, int x0, in
                 tpr = ur_read<R>(b, m, cell, s);
             } else {
                 const int r = pos - (y0 - 2);
-                const unsigned mx = (unsigned)sm[SM::MX_OFF + r * CP + (line - x0)];
+                const unsigned mx = reinterpret_cast<const unsigned char*>(sm + SM::TOTAL)[r * CP + (line - x0)];
                 tpl = sm[SM::SAX_OFF + (m * 31 + (pos - (y0 - 1))) * CP + (line - x0)];
                 tpr = ((mx >> m) & 1u) ? sm[SM::CRX_OFF + (m * 31 + r) * CP + (line - x0)] : ur_read<R>(b, m, cell, s);
             }
@@ -539,7 +540,7 @@ __device__ void sweep_line(const MixP<R>& P, const MixB<R>& b, R* sm, int x0, in
         // x candidates needed by the y sweep (URStar before the y sweep)
         const int r = line - (y0 - 2);
         if (r >= 0 && r < 31 && out_cell) {
-            sm[SM::MX_OFF + r * CP + (pos - x0)] = (R)cd.mask;
+            reinterpret_cast<unsigned char*>(sm + SM::TOTAL)[r * CP + (pos - x0)] = (unsigned char)cd.mask;
 #pragma unroll
             for (int m = 0; m < M; ++m) sm[SM::CRX_OFF + (m * 31 + r) * CP + (pos - x0)] = cd.Rr[m];
         }
@@ -581,7 +582,7 @@ __device__ void sweep_line(const MixP<R>& P, const MixB<R>& b, R* sm, int x0, in
                 for (int m = 0; m < M; ++m) sm[SM::SAX_OFF + (m * 31 + r) * CP + (pos - x0)] = astar[m];
         } else if (out_cell) {
 #pragma unroll
-            for (int m = 0; m < M; ++m) sm[SM::SAY_OFF + m * SM::CT + (pos - y0) * CP + (line - x0)] = astar[m];
+            for (int m = 0; m < M; ++m) b.starA[s & 1][(long long)m * b.N + line + (long long)P.nx * pos] = astar[m];
         }
         // ULStar ghost at the hi+1 face of the box to the face's left
         const bool line_out = D == 0 ? (line >= y0 && line < y0 + MT && line < P.ny) : true;
@@ -594,15 +595,18 @@ __device__ void sweep_line(const MixP<R>& P, const MixB<R>& b, R* sm, int x0, in
         }
         if (D == 1 && out_cell) {
             // the cell's URStar after this stage: y candidate, else x candidate
+            // (versioned by stage: readers of this stage see the previous value)
             const int r = pos - (y0 - 2);
-            const unsigned mxm = (unsigned)sm[SM::MX_OFF + r * CP + (line - x0)];
+            const unsigned mxm = reinterpret_cast<const unsigned char*>(sm + SM::TOTAL)[r * CP + (line - x0)];
             const unsigned f = cd.mask | mxm;
+            if (f) {
+                const long long cell = line + (long long)P.nx * pos;
 #pragma unroll
-            for (int m = 0; m < M; ++m) {
-                const R v = ((cd.mask >> m) & 1u) ? cd.Rr[m] : sm[SM::CRX_OFF + (m * 31 + r) * CP + (line - x0)];
-                sm[SM::URV_OFF + m * SM::CT + (pos - y0) * CP + (line - x0)] = v;
+                for (int m = 0; m < M; ++m)
+                    if ((f >> m) & 1u)
+                        ur_write<R>(b, m, cell, s,
+                                    ((cd.mask >> m) & 1u) ? cd.Rr[m] : sm[SM::CRX_OFF + (m * 31 + r) * CP + (line - x0)]);
             }
-            sm[SM::URF_OFF + (pos - y0) * CP + (line - x0)] = (R)f;
         }
     }
 
@@ -633,7 +637,7 @@ __device__ void sweep_line(const MixP<R>& P, const MixB<R>& b, R* sm, int x0, in
 }
 
 template <typename R, int M, bool THINC>
-__global__ void __launch_bounds__(NTH, sizeof(R) == 4 ? 2 : 1) k_stage2d(MixP<R> P, MixB<R> b, int stage)
+__global__ void __launch_bounds__(NTH, sizeof(R) == 4 ? 3 : 1) k_stage2d(MixP<R> P, MixB<R> b, int stage)
 {
     if (b.scal->done) return;
     using SM = Smem<R, M, THINC>;
@@ -815,16 +819,6 @@ __global__ void __launch_bounds__(NTH, sizeof(R) == 4 ? 2 : 1) k_stage2d(MixP<R>
         Xout[W_EH<M>() * N + g] = eh;
         Xout[W_EL<M>() * N + g] = el;
         Xout[W_P<M>() * N + g] = p;
-        if (THINC) {
-            const int par_out = s & 1;
-#pragma unroll
-            for (int m = 0; m < M; ++m) b.starA[par_out][(long long)m * N + g] = sm[SM::SAY_OFF + m * SM::CT + oc];
-            const unsigned f = (unsigned)sm[SM::URF_OFF + oc];
-            if (f)
-#pragma unroll
-                for (int m = 0; m < M; ++m)
-                    if ((f >> m) & 1u) ur_write<R>(b, m, g, s, sm[SM::URV_OFF + m * SM::CT + oc]);
-        }
     }
     if (stage == 1) {
         if (nan_seen) atomicOr(&b.scal->nan_flag, 1);

@@ -41,7 +41,7 @@ namespace tj {
 
 namespace {
 
-constexpr int NT3 = 256;
+constexpr int NT3 = 512;
 
 struct M3P {
     int M;
