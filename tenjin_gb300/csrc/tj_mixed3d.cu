@@ -421,7 +421,7 @@ __global__ void __launch_bounds__(NT3) k_stage3d(M3P P, M3B b, int stage, int fo
         const long long off = D.off;
         const int nx = D.n[0], ny = D.n[1], nz = D.n[2];
 
-#pragma unroll 1
+#pragma unroll
         for (int d = 0; d < 3; ++d) {
             const int fx = ex + (d == 0), fy = ey + (d == 1), fz = ez + (d == 2);
             const int stride = d == 0 ? 1 : (d == 1 ? SM::SX : SM::SX * SM::SY);
