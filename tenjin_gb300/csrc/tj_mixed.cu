@@ -380,6 +380,15 @@ __device__ __forceinline__ void thinc_cand_f(const MixP<R>& P, const R* sU, int 
     }
 }
 
+// Asynchronous global -> shared copy of one word (cp.async, 4 or 8 bytes).
+template <typename R>
+__device__ __forceinline__ void cp_async_r(R* dst, const R* src)
+{
+    const unsigned a = (unsigned)__cvta_generic_to_shared(dst);
+    if constexpr (sizeof(R) == 4) asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(a), "l"(src) : "memory");
+    else asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(a), "l"(src) : "memory");
+}
+
 // One sweep line (a row for D = 0, a column for D = 1) of 32 lanes.
 template <typename R, int M, bool THINC, int D>
 __device__ void sweep_line(const MixP<R>& P, const MixB<R>& b, R* sm, int x0, int y0, int line, int s, R dtdx,
@@ -652,43 +661,59 @@ __global__ void __launch_bounds__(NTH, sizeof(R) == 4 ? 3 : 1) k_stage2d(MixP<R>
     const R dtdx = sizeof(R) == 8 ? (R)(b.scal->dt / P.dxd[0]) : (R)b.scal->dt * P.idx[0];
     const R dtdy = sizeof(R) == 8 ? (R)(b.scal->dt / P.dxd[1]) : (R)b.scal->dt * P.idx[1];
 
-    // ---- stage the primitives of tile + halo ----
-#pragma unroll 5
+    // ---- stage the primitives of tile + halo and the output cells' conserved
+    //      words (U1 = U, hllc.cpp:583) with asynchronous copies: every copy is
+    //      in flight at once, none holds a register ----
     for (int t = threadIdx.x; t < MS * MS; t += NTH) {
         const int tx = t % MS, ty = t / MS;
         bool rx, ry;
         const int gx = reflect_map(x0 - MH + tx, P.nx, P.lo_bc[0], P.hi_bc[0], rx);
         const int gy = reflect_map(y0 - MH + ty, P.ny, P.lo_bc[1], P.hi_bc[1], ry);
         const long long g = gx + (long long)P.nx * gy;
+        R* Su = sm + SM::U_OFF + ty * MP + tx;
 #pragma unroll
         for (int m = 0; m < M; ++m) {
-            sm[SM::U_OFF + m * MS * MP + ty * MP + tx] = Xin[W_A(m) * N + g];
-            sm[SM::U_OFF + (M + m) * MS * MP + ty * MP + tx] = Xin[W_RK<M>(m) * N + g];
+            cp_async_r(Su + m * MS * MP, Xin + W_A(m) * N + g);
+            cp_async_r(Su + (M + m) * MS * MP, Xin + W_RK<M>(m) * N + g);
         }
-        const R u = Xin[W_U<M>(0) * N + g], v = Xin[W_U<M>(1) * N + g];
-        sm[SM::U_OFF + (2 * M) * MS * MP + ty * MP + tx] = rx ? -u : u;
-        sm[SM::U_OFF + (2 * M + 1) * MS * MP + ty * MP + tx] = ry ? -v : v;
-        sm[SM::U_OFF + (2 * M + 2) * MS * MP + ty * MP + tx] = Xin[W_P<M>() * N + g];
+        cp_async_r(Su + (2 * M) * MS * MP, Xin + W_U<M>(0) * N + g);
+        cp_async_r(Su + (2 * M + 1) * MS * MP, Xin + W_U<M>(1) * N + g);
+        cp_async_r(Su + (2 * M + 2) * MS * MP, Xin + W_P<M>() * N + g);
     }
-    // ---- conserved variables of the output cells: U1 = U (hllc.cpp:583) ----
-#pragma unroll 4
     for (int t = threadIdx.x; t < MT * MT; t += NTH) {
         const int ci = t % MT, cj = t / MT;
         const int gx = x0 + ci, gy = y0 + cj;
         if (gx >= P.nx || gy >= P.ny) continue;
         const long long g = gx + (long long)P.nx * gy;
-        const int oc = cj * CP + ci;
+        R* Sc = sm + SM::C_OFF + cj * CP + ci;
 #pragma unroll
         for (int m = 0; m < M; ++m) {
-            sm[SM::C_OFF + m * SM::CT + oc] = Xin[W_A(m) * N + g];
-            sm[SM::C_OFF + (M + m) * SM::CT + oc] = Xin[W_AR<M>(m) * N + g];
+            cp_async_r(Sc + m * SM::CT, Xin + W_A(m) * N + g);
+            cp_async_r(Sc + (M + m) * SM::CT, Xin + W_AR<M>(m) * N + g);
         }
-        sm[SM::C_OFF + (2 * M) * SM::CT + oc] = Xin[W_RU<M>(0) * N + g];
-        sm[SM::C_OFF + (2 * M + 1) * SM::CT + oc] = Xin[W_RU<M>(1) * N + g];
-        sm[SM::C_OFF + (2 * M + 2) * SM::CT + oc] = Xin[W_EH<M>() * N + g];
-        sm[SM::C_OFF + (2 * M + 3) * SM::CT + oc] = Xin[W_EL<M>() * N + g];
+        cp_async_r(Sc + (2 * M) * SM::CT, Xin + W_RU<M>(0) * N + g);
+        cp_async_r(Sc + (2 * M + 1) * SM::CT, Xin + W_RU<M>(1) * N + g);
+        cp_async_r(Sc + (2 * M + 2) * SM::CT, Xin + W_EH<M>() * N + g);
+        cp_async_r(Sc + (2 * M + 3) * SM::CT, Xin + W_EL<M>() * N + g);
     }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
     __syncthreads();
+    // reflect_odd ghosts (FillDomainBoundary): negate the normal velocity of
+    // staged cells that mirror across a reflective face
+    if ((P.lo_bc[0] == TJ_BC_REFLECTIVE && x0 < MH) || (P.hi_bc[0] == TJ_BC_REFLECTIVE && x0 - MH + MS > P.nx) ||
+        (P.lo_bc[1] == TJ_BC_REFLECTIVE && y0 < MH) || (P.hi_bc[1] == TJ_BC_REFLECTIVE && y0 - MH + MS > P.ny)) {
+        for (int t = threadIdx.x; t < MS * MS; t += NTH) {
+            const int tx = t % MS, ty = t / MS;
+            bool rx, ry;
+            reflect_map(x0 - MH + tx, P.nx, P.lo_bc[0], P.hi_bc[0], rx);
+            reflect_map(y0 - MH + ty, P.ny, P.lo_bc[1], P.hi_bc[1], ry);
+            R* Su = sm + SM::U_OFF + ty * MP + tx;
+            if (rx) Su[(2 * M) * MS * MP] = -Su[(2 * M) * MS * MP];
+            if (ry) Su[(2 * M + 1) * MS * MP] = -Su[(2 * M + 1) * MS * MP];
+        }
+        __syncthreads();
+    }
 
     const int warp = threadIdx.x >> 5;
     // ---- x sweep: rows ----
