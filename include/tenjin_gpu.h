@@ -135,6 +135,11 @@ int tj_set_primitive(tj_ctx* ctx, int domain, const double* prim);
 int tj_compute_dt(tj_ctx* ctx, double* dt);
 /* advance (hllc.cpp:699-707): two HLLCadvance stages and U1 = (U + U2)/2. */
 int tj_advance(tj_ctx* ctx, double dt);
+/* One RK stage of advance, for testing (FP64 precision only). stage 0: the
+ * state becomes U1 = HLLCadvance(U^n) (hllc.cpp:701), U^n is kept; stage 1:
+ * the state becomes U^n/2 + HLLCadvance(U1)/2 (703-705). Stage 0 then stage
+ * 1 with the same dt equals tj_advance. */
+int tj_advance_stage(tj_ctx* ctx, int stage, double dt);
 /* PlasticEOS::plasticUpdate (plastic.cpp:227-244), radial return. */
 int tj_plastic_update(tj_ctx* ctx, double dt);
 /* geometricSourceTerm (radial.cpp:37-54): the radial source of a spherical

@@ -62,6 +62,7 @@ SIGNATURES = [
     ("tj_set_primitive", _I, [_P, _I, _PD]),
     ("tj_compute_dt", _I, [_P, _PD]),
     ("tj_advance", _I, [_P, _D]),
+    ("tj_advance_stage", _I, [_P, _I, _D]),
     ("tj_plastic_update", _I, [_P, _D]),
     ("tj_reactive_update", _I, [_P, _D]),
     ("tj_geometric_source", _I, [_P, _D]),

@@ -108,6 +108,7 @@ struct tj_ctx {
     // fused kernels' state (precisions MIXED / FUSED64); conversions are made
     // when the other copy is next needed, not per call
     bool a_current = true, x_current = true;
+    bool stage0_done = false;  // tj_advance_stage(0) saved U^n in C for stage 1
     // device memory
     DevDomain* d_doms = nullptr;
     int* d_boxes = nullptr;
@@ -775,6 +776,35 @@ int tj_advance(tj_ctx* c, double dt)
     // the post-advance operators, which have their own entry points.
     c->launches += fp64_stage(c->P, b, c->A, c->B, 0, c->stream);
     c->launches += fp64_stage(c->P, b, c->B, c->C, 2, c->stream);
+    TJ_CUDA(c, cudaGetLastError());
+    return check_status(c);
+}
+
+int tj_advance_stage(tj_ctx* c, int stage, double dt)
+{
+    if (!c || (stage != 0 && stage != 1)) return TJ_ERR_ARG;
+    int e = need_state(c);
+    if (e) return e;
+    if (is_mixed(c)) return fail(c, TJ_ERR_ARG, "tj_advance_stage is FP64-only");
+    Fp64Bufs b = bufs(c);
+    const size_t bytes = sizeof(double) * (size_t)c->P.NS * (size_t)c->ntot;
+    c->launches += fp64_set_dt(b, dt, c->stream);
+    if (stage == 0) {
+        // U^n is kept in C for the second stage's average; the state becomes
+        // U1 = HLLCadvance(U^n)
+        TJ_CUDA(c, cudaMemcpyAsync(c->C, c->A, bytes, cudaMemcpyDeviceToDevice, c->stream));
+        c->launches += fp64_stage(c->P, b, c->A, c->B, 0, c->stream);
+        TJ_CUDA(c, cudaMemcpyAsync(c->A, c->B, bytes, cudaMemcpyDeviceToDevice, c->stream));
+        c->stage0_done = true;
+    } else {
+        if (!c->stage0_done) return fail(c, TJ_ERR_STATE, "tj_advance_stage(1) follows tj_advance_stage(0)");
+        // U2 = HLLCadvance(U1), then U1 = U^n/2 + U2/2 (hllc.cpp:701-705)
+        Fp64Bufs bb = b;
+        bb.A = c->C;
+        c->launches += fp64_stage(c->P, bb, c->A, c->B, 2, c->stream);
+        TJ_CUDA(c, cudaMemcpyAsync(c->A, c->C, bytes, cudaMemcpyDeviceToDevice, c->stream));
+        c->stage0_done = false;
+    }
     TJ_CUDA(c, cudaGetLastError());
     return check_status(c);
 }

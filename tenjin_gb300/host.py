@@ -134,6 +134,10 @@ class TenjinGPU:
     def advance(self, dt: float):
         self._check(self.L.tj_advance(self.h, float(dt)))
 
+    def advance_stage(self, stage: int, dt: float):
+        """One RK stage of advance (HLLCadvance, hllc.cpp:701-705), FP64 only."""
+        self._check(self.L.tj_advance_stage(self.h, int(stage), float(dt)))
+
     def plasticUpdate(self, dt: float = 0.0):
         self._check(self.L.tj_plastic_update(self.h, float(dt)))
 
