@@ -2,9 +2,9 @@
 // flux, update), one source for two working types: PT = DevParams (binary64,
 // the reference's evaluation order: bit-exact parity, compiled with
 // -fmad=false in tj_fp64.cu) and PT = DevParams32 (binary32 bulk, tj_fp32.cu).
-// The binary32 instance keeps the total energy as a compensated pair (E, Elo),
-// closes the pressure in binary64 (in c2p) and projects onto the yield
-// surface in binary64 (plastic_cell_in64); everything else is the same code.
+// The binary32 instance keeps the total energy as a compensated pair (E, Elo)
+// and closes the pressure in binary64 (in c2p); everything else is the same
+// code.
 //
 // One RK stage (HLLCadvance, hllc.cpp:579-695) is, per direction d:
 //   k_recon   per cell : MUSCL (hllc.cpp:541-575), BVD-THINC (thinc.cpp:67-208),
@@ -855,65 +855,6 @@ __device__ inline void cleanup_v_cell(const PT& P, CellT<R>& c)
         for (int q = 0; q < 3; ++q) c.V[3 * r + q] = ((Sq[3 * r + q] * norm * ts) + (R)(r == q) * (ta - ts)) / ta;
 }
 
-// The radial return of a binary32 cell in binary64 (the yield projection),
-// followed by conservativeToPrimitive in binary64 (plastic.cpp:227-244).
-template <typename PT, typename R = typename PT::real>
-__device__ inline int plastic_cell_in64(const PT& P, CellT<R>& c)
-{
-    CellT<double> d;
-    const DevParams& PD = P.d;
-    for (int m = 0; m < P.M; ++m) {
-        d.alpha[m] = c.alpha[m];
-        d.arho[m] = c.arho[m];
-        d.rhok[m] = c.rhok[m];
-        d.eps[m] = c.eps[m];
-        d.are[m] = c.are[m];
-    }
-    d.rho = c.rho;
-#pragma unroll
-    for (int r = 0; r < 3; ++r) {
-        d.rhou[r] = c.rhou[r];
-        d.vel[r] = c.vel[r];
-    }
-    d.E = (double)c.E + (double)c.Elo;
-    d.Elo = 0.0;
-    d.p = c.p;
-    d.a = c.a;
-    d.hj2 = c.hj2;
-#pragma unroll
-    for (int q = 0; q < 9; ++q) {
-        d.sigma[q] = c.sigma[q];
-        d.V[q] = c.V[q];
-        d.devH[q] = c.devH[q];
-    }
-    const int e = plastic_cell(PD, d);
-    c2p(PD, d);
-    for (int m = 0; m < P.M; ++m) {
-        c.alpha[m] = (R)d.alpha[m];
-        c.arho[m] = (R)d.arho[m];
-        c.rhok[m] = (R)d.rhok[m];
-        c.eps[m] = (R)d.eps[m];
-        c.are[m] = (R)d.are[m];
-    }
-    c.rho = (R)d.rho;
-#pragma unroll
-    for (int r = 0; r < 3; ++r) {
-        c.rhou[r] = (R)d.rhou[r];
-        c.vel[r] = (R)d.vel[r];
-    }
-    c.E = (R)d.E;
-    c.Elo = (R)(d.E - (double)c.E);
-    c.p = (R)d.p;
-    c.hj2 = (R)d.hj2;
-#pragma unroll
-    for (int q = 0; q < 9; ++q) {
-        c.sigma[q] = (R)d.sigma[q];
-        c.V[q] = (R)d.V[q];
-        c.devH[q] = (R)d.devH[q];
-    }
-    return e;
-}
-
 // contains_nan over the conservative and primitive lists of one cell.
 template <typename PT, typename R = typename PT::real>
 __device__ inline bool cell_has_nan(const PT& P, const CellT<R>& c)
@@ -1091,11 +1032,8 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1)
                 }
                 if (P.plastic) {
                     int e;
-                    if constexpr (sizeof(R) == 4) e = plastic_cell_in64(P, Yc);
-                    else {
-                        e = plastic_cell(P, Yc);
-                        c2p(P, Yc);
-                    }
+                    e = plastic_cell(P, Yc);
+                    c2p(P, Yc);
                     if (e) set_status(b.scal, e);
                 }
                 if (P.radial) {

@@ -2,7 +2,7 @@
 fused kernels do not cover): solids with the 5-wave solver, plasticity and
 cleanUpV, the 1-D shock tube, several 2-D domains. Against the FP64 path on
 the same inputs: relative L1 density error <= 1e-4 (the pressure closure and
-the yield projection run in binary64, the energy is a compensated pair)."""
+the pressure closure runs in binary64, the energy is a compensated pair)."""
 import numpy as np
 import pytest
 
