@@ -583,15 +583,15 @@ __device__ void sweep_line(const MixP<R>& P, const MixB<R>& b, R* sm, int x0, in
     const bool hi_face = pos == n && lane >= 3 && lane <= 30;
     if (THINC) {
         // star alpha: x faces kept in shared memory (rows y0-1..y0+29) for
-        // the y sweep; y faces of output cells go out as the next stage's ULStar
-        if (D == 0) {
-            const int r = line - (y0 - 1);
+        // the y sweep; the y faces of output cells (the next stage's ULStar)
+        // take their cell's place in the same array: each y-sweep warp reads
+        // only its own column of it, and all its reads come before this write
+        if (D == 0 || out_cell) {
+            const int r = D == 0 ? line - (y0 - 1) : pos - (y0 - 1);
+            const int col = D == 0 ? pos - x0 : line - x0;
             if (r >= 0 && r < 31 && out_cell)
 #pragma unroll
-                for (int m = 0; m < M; ++m) sm[SM::SAX_OFF + (m * 31 + r) * CP + (pos - x0)] = astar[m];
-        } else if (out_cell) {
-#pragma unroll
-            for (int m = 0; m < M; ++m) b.starA[s & 1][(long long)m * b.N + line + (long long)P.nx * pos] = astar[m];
+                for (int m = 0; m < M; ++m) sm[SM::SAX_OFF + (m * 31 + r) * CP + col] = astar[m];
         }
         // ULStar ghost at the hi+1 face of the box to the face's left
         const bool line_out = D == 0 ? (line >= y0 && line < y0 + MT && line < P.ny) : true;
@@ -844,6 +844,10 @@ __global__ void __launch_bounds__(NTH, sizeof(R) == 4 ? 3 : 1) k_stage2d(MixP<R>
         Xout[W_EH<M>() * N + g] = eh;
         Xout[W_EL<M>() * N + g] = el;
         Xout[W_P<M>() * N + g] = p;
+        if (THINC)
+#pragma unroll
+            for (int m = 0; m < M; ++m)
+                b.starA[s & 1][(long long)m * N + g] = sm[SM::SAX_OFF + (m * 31 + (cj + 1)) * CP + ci];
     }
     if (stage == 1) {
         if (nan_seen) atomicOr(&b.scal->nan_flag, 1);
