@@ -114,8 +114,12 @@ int tj_get_box(const tj_ctx* ctx, int domain, int box, int* lohi);
 int tj_num_cells(const tj_ctx* ctx, long long* ncells);
 
 /* State exchange in the reference's FArrayBox layout (box grown by ngrow,
- * ncomp must equal tj_ncomp). Upload reads the valid cells; download writes
- * the valid cells (ghosts untouched). */
+ * ncomp must equal tj_ncomp). Upload reads the valid cells of the components
+ * the update carries from step to step (alpha, alphaRho, rho_k, rho, rhoU, u,
+ * E, p, and rhomix, lambda, alphaRhoLambda, V, HenckyJ2, epsilon,
+ * alphaRhoEpsilon where present); the derived ones (a, uStar, sigma, VStar,
+ * devH) are recomputed on the device and not read. Download writes every
+ * component of the valid cells (ghosts untouched). */
 int tj_upload_state(tj_ctx* ctx, int domain, int box, const double* fab, int ncomp, int ngrow);
 int tj_download_state(tj_ctx* ctx, int domain, int box, double* fab, int ncomp, int ngrow);
 /* Whole-domain exchange: ncomp blocks of nx*ny*nz doubles (valid cells, i
