@@ -123,6 +123,7 @@ struct tj_ctx {
     static constexpr int kSlabs = 8;
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t slab_ev[kSlabs + 1] = {};
+    int coherent_host = -1;  // device reads host memory coherently (unknown until asked)
     MixedState mixed;
     // graph-captured step groups
     cudaGraphExec_t graph_exec = nullptr;
@@ -624,6 +625,32 @@ static int ensure_staging(tj_ctx* c, size_t bytes)
     return TJ_OK;
 }
 
+// The device address of a host buffer the conversion kernels may read and
+// write in place, or null. Taken when the device accesses host memory
+// coherently (a Grace host over NVLink-C2C: any valid host address is legal
+// there) and both ends of the buffer are page-locked and mapped at the same
+// offset: the kernels then move each byte across the link once, at the
+// link's rate, with no staging copy and no separate conversion pass.
+static double* mapped_view(tj_ctx* c, double* host, size_t bytes)
+{
+    if (c->coherent_host < 0) {
+        int dev = 0, v = 0;
+        c->coherent_host = cudaGetDevice(&dev) == cudaSuccess &&
+                           cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, dev) == cudaSuccess && v == 1;
+    }
+    if (!c->coherent_host || bytes == 0) return nullptr;
+    cudaPointerAttributes a{}, z{};
+    const char* last = reinterpret_cast<const char*>(host) + bytes - 1;
+    if (cudaPointerGetAttributes(&a, host) != cudaSuccess || cudaPointerGetAttributes(&z, last) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type != cudaMemoryTypeHost || z.type != cudaMemoryTypeHost || !a.devicePointer ||
+        static_cast<const char*>(z.devicePointer) != static_cast<const char*>(a.devicePointer) + (bytes - 1))
+        return nullptr;
+    return static_cast<double*>(a.devicePointer);
+}
+
 static int exchange(tj_ctx* c, int q, const int* bx, double* host, int ncomp, int ngrow, bool up)
 {
     int e = need_state(c);
@@ -635,9 +662,34 @@ static int exchange(tj_ctx* c, int q, const int* bx, double* host, int ncomp, in
     int ld_k = bx[5] - bx[2] + 1 + (dim > 2 ? 2 * ngrow : 0);
     long long cs = (long long)ld_i * ld_j * ld_k;
     size_t bytes = sizeof(double) * ncomp * cs;
+    Fp64Bufs b = bufs(c);
+    if (double* dv = mapped_view(c, host, bytes)) {
+        // in place: the kernels read (write) the caller's page-locked buffer
+        if (up) {
+            const DevDomain& Dq = c->doms[q];
+            const bool whole = c->doms.size() == 1 && bx[0] == 0 && bx[1] == 0 && bx[2] == 0 &&
+                               bx[3] == Dq.n[0] - 1 && bx[4] == Dq.n[1] - 1 && bx[5] == Dq.n[2] - 1;
+            if (!whole) a_sync(c);
+            // the fused 2-D state is filled in the same pass (no conversion
+            // before the next step)
+            const int r = whole && ngrow == 0 && is_mixed(c) ? mixed_from_ap(c->mixed, c->P, b, dv, c->stream) : -1;
+            if (r >= 0) {
+                c->launches += r;
+                c->a_current = c->x_current = true;
+            } else {
+                c->launches += fp64_ap_to_state(c->P, b, q, bx, dv, ld_i, ld_j, ld_k, cs, ngrow, c->A, c->stream);
+                a_written(c);
+            }
+        } else {
+            a_sync(c);
+            c->launches += fp64_state_to_ap(c->P, b, q, bx, c->A, dv, ld_i, ld_j, ld_k, cs, ngrow, c->stream);
+        }
+        TJ_CUDA(c, cudaStreamSynchronize(c->stream));
+        TJ_CUDA(c, cudaGetLastError());
+        return TJ_OK;
+    }
     e = ensure_staging(c, bytes);
     if (e) return e;
-    Fp64Bufs b = bufs(c);
     if (up) {
         // the cells outside this box keep their current values; a box that is
         // the whole of the only domain replaces the state entirely

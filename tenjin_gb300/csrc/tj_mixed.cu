@@ -932,6 +932,61 @@ __global__ void k_from_fp64(DevParams DP, MixB<R> b, const double* A, int* bad)
     }
 }
 
+// The whole domain in AccessPattern planes (component c of cell g at
+// ap[c * N + g], with ngrow 0) -> the FP64 carried state and the fused state
+// in one pass. ap may be a page-locked host buffer read in place: each thread
+// issues all of a cell's loads before its stores, so that many are in flight
+// over the host link. The values written are those of k_ap_to_state followed
+// by k_from_fp64.
+template <typename R, int M>
+__global__ void k_from_ap(DevParams DP, MixB<R> b, const double* __restrict__ ap, double* __restrict__ A, int* bad)
+{
+    const long long N = b.N;
+    R* __restrict__ X = b.X[0];
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < N; g += (long long)gridDim.x * blockDim.x) {
+        double al[M], ar[M], rk[M], ru[3], u[3];
+#pragma unroll
+        for (int m = 0; m < M; ++m) {
+            al[m] = ap[(DP.A_ALPHA + m) * N + g];
+            ar[m] = ap[(DP.A_ARHO + m) * N + g];
+            rk[m] = ap[(DP.A_RHOK + m) * N + g];
+        }
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            ru[r] = ap[(DP.A_RHOU + r) * N + g];
+            u[r] = ap[(DP.A_VEL + r) * N + g];
+        }
+        const double rho = ap[DP.A_RHO * N + g], E = ap[DP.A_E * N + g], p = ap[DP.A_P * N + g];
+#pragma unroll
+        for (int m = 0; m < M; ++m) {
+            A[(DP.S_ALPHA + m) * N + g] = al[m];
+            A[(DP.S_ARHO + m) * N + g] = ar[m];
+            A[(DP.S_RHOK + m) * N + g] = rk[m];
+            X[W_A(m) * N + g] = (R)al[m];
+            X[W_AR<M>(m) * N + g] = (R)ar[m];
+            X[W_RK<M>(m) * N + g] = (R)rk[m];
+        }
+        A[DP.S_RHO * N + g] = rho;
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            A[(DP.S_RHOU + r) * N + g] = ru[r];
+            A[(DP.S_VEL + r) * N + g] = u[r];
+        }
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+            X[W_RU<M>(r) * N + g] = (R)ru[r];
+            X[W_U<M>(r) * N + g] = (R)u[r];
+        }
+        A[DP.S_E * N + g] = E;
+        const R eh = (R)E;
+        X[W_EH<M>() * N + g] = eh;
+        X[W_EL<M>() * N + g] = (R)(E - (double)eh);
+        A[DP.S_P * N + g] = p;
+        X[W_P<M>() * N + g] = (R)p;
+        if (u[2] != 0.0 || ru[2] != 0.0) atomicOr(bad, 1);
+    }
+}
+
 template <typename R, int M>
 __global__ void k_to_fp64(DevParams DP, MixB<R> b, double* A)
 {
@@ -995,6 +1050,7 @@ struct MixedImpl : MixedBase {
     int* bx[4] = {nullptr, nullptr, nullptr, nullptr};
     int* ctr = nullptr;
     int* bad = nullptr;
+    int* bad_h = nullptr;  // page-locked copy of bad
 
     ~MixedImpl() override
     {
@@ -1004,6 +1060,7 @@ struct MixedImpl : MixedBase {
         int* is[] = {urs[0], urs[1], bx[0], bx[1], bx[2], bx[3], ctr, bad};
         for (int* p : is)
             if (p) cudaFree(p);
+        if (bad_h) cudaFreeHost(bad_h);
     }
 
     int alloc(const DevParams& DP, const DevDomain& D, long long N, cudaStream_t st)
@@ -1065,6 +1122,8 @@ struct MixedImpl : MixedBase {
         cudaMemsetAsync(ctr, 0, sizeof(int), st);
         if (cudaMalloc(&bad, sizeof(int)) != cudaSuccess) return TJ_ERR_CUDA;
         cudaMemsetAsync(bad, 0, sizeof(int), st);
+        if (cudaMallocHost(&bad_h, sizeof(int)) != cudaSuccess) return TJ_ERR_CUDA;
+        *bad_h = 0;
         for (int q = 0; q < 2; ++q) {
             b.X[q] = X[q];
             b.starA[q] = starA[q];
@@ -1130,11 +1189,30 @@ struct MixedImpl : MixedBase {
             case 3: k_from_fp64<R, 3><<<nblk(b.N), 256, 0, st>>>(DP, b, fb.A, bad); break;
             default: k_from_fp64<R, 4><<<nblk(b.N), 256, 0, st>>>(DP, b, fb.A, bad); break;
         }
-        int hbad = 0;
-        cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, st);
+        return 1 + cfl(fb, st) + report_w(st);
+    }
+
+    int from_ap(const DevParams& DP, const Fp64Bufs& fb, const double* ap, cudaStream_t st) override
+    {
+        b.scal = fb.scal;
+        cudaMemsetAsync(bad, 0, sizeof(int), st);
+        switch (M) {
+            case 1: k_from_ap<R, 1><<<nblk(b.N), 256, 0, st>>>(DP, b, ap, fb.A, bad); break;
+            case 2: k_from_ap<R, 2><<<nblk(b.N), 256, 0, st>>>(DP, b, ap, fb.A, bad); break;
+            case 3: k_from_ap<R, 3><<<nblk(b.N), 256, 0, st>>>(DP, b, ap, fb.A, bad); break;
+            default: k_from_ap<R, 4><<<nblk(b.N), 256, 0, st>>>(DP, b, ap, fb.A, bad); break;
+        }
+        return 1 + cfl(fb, st) + report_w(st);
+    }
+
+    // waits for the stream; warns when an uploaded cell had a third velocity
+    // component, which the 2-D fused state does not carry
+    int report_w(cudaStream_t st)
+    {
+        cudaMemcpyAsync(bad_h, bad, sizeof(int), cudaMemcpyDeviceToHost, st);
         cudaStreamSynchronize(st);
-        if (hbad) std::fprintf(stderr, "tenjin_gpu: the fused 2-D kernels carry two velocity components; w was nonzero\n");
-        return 1 + cfl(fb, st);
+        if (*bad_h) std::fprintf(stderr, "tenjin_gpu: the fused 2-D kernels carry two velocity components; w was nonzero\n");
+        return 0;
     }
 
     int to_fp64(const DevParams& DP, const Fp64Bufs& fb, cudaStream_t st) override
@@ -1291,6 +1369,11 @@ void mixed_describe(const MixedState& ms, char* buf, size_t len)
 int mixed_from_fp64(MixedState& ms, const DevParams& DP, const Fp64Bufs& fb, cudaStream_t st)
 {
     return ((MixedBase*)ms.impl)->from_fp64(DP, fb, st);
+}
+
+int mixed_from_ap(MixedState& ms, const DevParams& DP, const Fp64Bufs& fb, const double* ap, cudaStream_t st)
+{
+    return ((MixedBase*)ms.impl)->from_ap(DP, fb, ap, st);
 }
 
 int mixed_to_fp64(MixedState& ms, const DevParams& DP, const Fp64Bufs& fb, cudaStream_t st)

@@ -21,6 +21,15 @@ struct MixedBase {
                           cudaStream_t st) = 0;
     virtual int from_fp64(const DevParams& DP, const Fp64Bufs& fb, cudaStream_t st) = 0;
     virtual int to_fp64(const DevParams& DP, const Fp64Bufs& fb, cudaStream_t st) = 0;
+    // Whole-domain AccessPattern planes (ngrow 0, possibly a page-locked host
+    // buffer read in place) -> both the FP64 carried state and the mixed state,
+    // the next step's CFL minimum armed; returns the launches, -1 where the
+    // implementation has no such pass. Waits for the stream.
+    virtual int from_ap(const DevParams& DP, const Fp64Bufs& fb, const double* ap, cudaStream_t st)
+    {
+        (void)DP, (void)fb, (void)ap, (void)st;
+        return -1;
+    }
     virtual int cfl(const Fp64Bufs& fb, cudaStream_t st) = 0;
     virtual int step(const DevParams& DP, const Fp64Bufs& fb, cudaStream_t st, Prof* pr) = 0;
     // a one-line description of the launch configuration in use
@@ -47,6 +56,7 @@ int mixed_set_boxes(MixedState& m, const DevParams& P, const std::vector<DevDoma
 // the next step's CFL minimum; and back.
 int mixed_from_fp64(MixedState& m, const DevParams& P, const Fp64Bufs& b, cudaStream_t st);
 int mixed_to_fp64(MixedState& m, const DevParams& P, const Fp64Bufs& b, cudaStream_t st);
+int mixed_from_ap(MixedState& m, const DevParams& P, const Fp64Bufs& b, const double* ap, cudaStream_t st);
 // CFL minimum of the current mixed state into DevScalars::dtmin_bits.
 int mixed_compute_dt(MixedState& m, const DevParams& P, const Fp64Bufs& b, cudaStream_t st);
 int mixed_step(MixedState& m, const DevParams& P, const Fp64Bufs& b, cudaStream_t st, Prof* pr = nullptr);

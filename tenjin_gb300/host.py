@@ -107,9 +107,15 @@ class TenjinGPU:
         prim = np.ascontiguousarray(prim, dtype=np.float64)
         self._check(self.L.tj_set_primitive(self.h, q, _dp(prim)))
 
-    def state(self, q: int = 0) -> np.ndarray:
+    def state(self, q: int = 0, out: Optional[np.ndarray] = None) -> np.ndarray:
+        """Domain q in AccessPattern layout (Ncomp planes of float64), into
+        `out` when given (C-contiguous float64 of that shape, e.g. a
+        page-locked buffer)."""
         d = self.case.domains[q]
-        out = np.empty((self.ncomp, d.n_cells[2], d.n_cells[1], d.n_cells[0]), dtype=np.float64)
+        shape = (self.ncomp, d.n_cells[2], d.n_cells[1], d.n_cells[0])
+        if out is None:
+            out = np.empty(shape, dtype=np.float64)
+        assert out.shape == shape and out.flags["C_CONTIGUOUS"] and out.dtype == np.float64
         self._check(self.L.tj_download_domain(self.h, q, _dp(out)))
         return out
 
