@@ -371,28 +371,27 @@ __device__ inline void sym3_eig(const R* a_in, R* w, R* q)
             }
         }
     }
-    int o0 = 0, o1 = 1, o2 = 2;
+    // decreasing order by an exchange sort on positions (0,1,2) that swaps
+    // the eigenvalues and their columns themselves (every index is a
+    // compile-time constant, so nothing leaves the registers)
     R d[3] = {a[0], a[4], a[8]};
-    // selection order identical to a stable exchange sort on (0,1,2)
-    int order[3] = {o0, o1, o2};
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
         for (int j = i + 1; j < 3; ++j)
-            if (d[order[j]] > d[order[i]]) {
-                int t = order[i];
-                order[i] = order[j];
-                order[j] = t;
+            if (d[j] > d[i]) {
+                const R t = d[i];
+                d[i] = d[j];
+                d[j] = t;
+#pragma unroll
+                for (int r = 0; r < 3; ++r) {
+                    const R u = q[r * 3 + i];
+                    q[r * 3 + i] = q[r * 3 + j];
+                    q[r * 3 + j] = u;
+                }
             }
-    R qs[9];
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        w[c] = d[order[c]];
-#pragma unroll
-        for (int r = 0; r < 3; ++r) qs[r * 3 + c] = q[r * 3 + order[c]];
-    }
-#pragma unroll
-    for (int i = 0; i < 9; ++i) q[i] = qs[i];
+    for (int c = 0; c < 3; ++c) w[c] = d[c];
 }
 
 // matrixSquareRoot (tensor.cpp:452-475): L S^(1/2) RT with L = Q, RT = Q^T.

@@ -178,7 +178,7 @@ struct General32 : MixedBase {
 
     void describe(char* buf, size_t len) const override
     {
-        std::snprintf(buf, len, "binary32 per-direction kernels (%d-D), binary64 pressure closure", P.dim);
+        std::snprintf(buf, len, "binary32 per-direction kernels (%d-D), binary64 pressure closure and plastic return map", P.dim);
     }
 };
 

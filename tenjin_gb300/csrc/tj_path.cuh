@@ -2,9 +2,9 @@
 // flux, update), one source for two working types: PT = DevParams (binary64,
 // the reference's evaluation order: bit-exact parity, compiled with
 // -fmad=false in tj_fp64.cu) and PT = DevParams32 (binary32 bulk, tj_fp32.cu).
-// The binary32 instance keeps the total energy as a compensated pair (E, Elo)
-// and closes the pressure in binary64 (in c2p); everything else is the same
-// code.
+// The binary32 instance keeps the total energy as a compensated pair (E, Elo),
+// closes the pressure in binary64 (in c2p) and runs the plastic return map in
+// binary64 (plastic_cell_proj64); everything else is the same code.
 //
 // One RK stage (HLLCadvance, hllc.cpp:579-695) is, per direction d:
 //   k_recon   per cell : MUSCL (hllc.cpp:541-575), BVD-THINC (thinc.cpp:67-208),
@@ -837,6 +837,75 @@ __device__ inline int plastic_cell(const PT& P, CellT<R>& c)
     return 0;
 }
 
+// The radial return of a binary32 cell with its return map in binary64
+// (plastic.cpp:83-223): the Hencky strain of V is binary32; J = sqrt(HJ2),
+// the projection J -> J_new onto the yield surface, the plastic strain and
+// alphaRhoEpsilon, the mixture-weighted scale JTotal / JBefore and the
+// scaled devH are binary64 from the binary64 EOS parameters, rounded back
+// once; the reconstruction of V from devH and the conservativeToPrimitive
+// that follows are binary32 (pressure closure in binary64).
+template <typename PT, typename R = typename PT::real>
+__device__ inline int plastic_cell_proj64(const PT& P, CellT<R>& c)
+{
+    const DevParams& PD = P.d;
+    R tsolid = R(0.0);
+    for (int m = 0; m < P.M; ++m)
+        if (P.phase[m] == TJ_PHASE_SOLID) tsolid += c.alpha[m];
+    if (tsolid <= R(0.5)) {  // cellIsMostlyFluid
+        for (int m = 0; m < P.M; ++m) { c.eps[m] = R(0.0); c.are[m] = R(0.0); }
+        return 0;
+    }
+    hencky(P, c);
+    const double hj2 = c.hj2;
+    double JT = 0.0, JB = 0.0, norm = 0.0;
+    for (int m = 0; m < P.M; ++m) {
+        ECellT<double> e;
+        e.alpha = c.alpha[m];
+        e.arho = c.arho[m];
+        e.rhok = c.rhok[m];
+        e.p = c.p;
+        e.hj2 = hj2;
+        e.lam = c.lam;
+        e.rm0 = c.rm0;
+        e.rm1 = c.rm1;
+        double J, Jn;
+        if (P.phase[m] == TJ_PHASE_SOLID) {
+            J = sqrt(hj2);
+            const double G = eos_G(PD, m, e);
+            Jn = (G * J * sqrt(3.0) > PD.yield[m]) ? PD.yield[m] / (sqrt(3.0) * G) : J;
+            const double eps = (double)c.eps[m] + sqrt(2.0 / 3.0) * (J - Jn);
+            c.eps[m] = (R)eps;
+            c.are[m] = (R)(eps * (double)c.arho[m]);
+        } else {
+            J = 0.0;
+            Jn = 0.0;
+            c.eps[m] = R(0.0);
+            c.are[m] = R(0.0);
+        }
+        const double ig = eos_invG(PD, m, e);
+        JB += ig * J;
+        JT += ig * Jn;
+        norm += ig;
+    }
+    JB *= 1.0 / norm;
+    JT *= 1.0 / norm;
+    if (JB == 0.0 && JT == 0.0) { JB = 1.0; JT = 1.0; }
+    R t1[9], t2[9], t2i[9];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            R& dv = c.devH[3 * r + q];
+            if (dv != R(0.0) && JB == 0.0 && JT != 0.0) return TJ_ERR_PLASTIC;
+            dv = (R)((double)dv * (JT / JB));
+            t1[3 * r + q] = (R)(r == q) + R(0.5) * dv;
+            t2[3 * r + q] = (R)(r == q) - R(0.5) * dv;
+        }
+    invert3(t2, t2i);
+    mm3(t2i, t1, c.V);
+    return 0;
+}
+
 template <typename PT, typename R = typename PT::real>
 __device__ inline void cleanup_v_cell(const PT& P, CellT<R>& c)
 {
@@ -1032,7 +1101,8 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1)
                 }
                 if (P.plastic) {
                     int e;
-                    e = plastic_cell(P, Yc);
+                    if constexpr (sizeof(R) == 4) e = plastic_cell_proj64(P, Yc);
+                    else e = plastic_cell(P, Yc);
                     c2p(P, Yc);
                     if (e) set_status(b.scal, e);
                 }
