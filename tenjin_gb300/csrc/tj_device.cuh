@@ -555,6 +555,43 @@ __device__ inline int mix_root_find(const PD& P, CellT<double>& c, double ke)
     return TJ_ERR_ROOT;
 }
 
+// The non-thermal energy, non-thermal pressure and alpha/Gamma terms of one
+// material for the binary64 pressure closure of a binary32 cell: the
+// formulas of eos_e_cold + eos_e_shear, eos_p_cold + eos_p_shear and
+// eos_invG, with each quotient formed once and the constant ones taken from
+// the precomputed reciprocals (a stiffened gas: one division, the Hugoniot
+// curve: three, against three and eight); other EOS go through the general
+// functions.
+template <typename P32>
+__device__ inline void closure_terms64(const P32& P, int m, const ECellT<double>& e, double& ent, double& pnt,
+                                       double& ig)
+{
+    const double* q = P.d.prm[m];
+    switch (P.d.eos[m]) {
+        case TJ_EOS_MIEGRUNEISEN: {
+            const double aG = e.alpha * P.rG[m];
+            ent += q[2] * e.arho;
+            pnt += q[1] * aG;
+            ig += aG;
+            return;
+        }
+        case TJ_EOS_HUGONIOT: {
+            const double aG = e.alpha * P.rG[m];
+            const double r0 = q[4], c0 = q[5], sl = q[6];
+            const double et = 1.0 - r0 / e.rhok, dd = 1.0 - sl * et;
+            const double ph = r0 * c0 * c0 * et / (dd * dd);
+            ent += e.arho * (ph * et * P.rR0h[m]) + e.alpha * (q[7] * e.hj2);
+            pnt += aG * ph - aG * (q[7] * e.hj2);
+            ig += aG;
+            return;
+        }
+        default:
+            ent += eos_e_cold(P.d, m, e) + eos_e_shear(P.d, m, e);
+            pnt += eos_p_cold(P.d, m, e) + eos_p_shear(P.d, m, e);
+            ig += eos_invG(P.d, m, e);
+    }
+}
+
 // conservativeToPrimitive (:67-122). Returns 0, or TJ_ERR_ROOT from the
 // mixture closure.
 template <typename PT>
@@ -579,13 +616,10 @@ __device__ inline int c2p(const PT& P, CellT<typename PT::real>& c)
         // binary32 state: the closure of the pressure (and of the mixture
         // densities) in binary64, from the compensated energy (E, Elo) and
         // binary64 cold terms
-        double rho = 0.0, ked = 0.0, ent = 0.0, pnt = 0.0, ig = 0.0;
+        double rho = 0.0, ent = 0.0, pnt = 0.0, ig = 0.0;
         for (int m = 0; m < P.M; ++m) rho += (double)c.arho[m];
-#pragma unroll
-        for (int r = 0; r < 3; ++r) {
-            const double u = (double)c.rhou[r] / rho;
-            ked += 0.5 * rho * u * u;
-        }
+        const double ru0 = c.rhou[0], ru1 = c.rhou[1], ru2 = c.rhou[2];
+        const double ked = 0.5 * (ru0 * ru0 + ru1 * ru1 + ru2 * ru2) / rho;
         double lam = 0.0, rm0 = 0.0, rm1 = 0.0;
         if (P.nmix) {
             lam = (double)c.arl / (double)c.arho[0];
@@ -618,9 +652,13 @@ __device__ inline int c2p(const PT& P, CellT<typename PT::real>& c)
             e.lam = lam;
             e.rm0 = rm0;
             e.rm1 = rm1;
-            ent += eos_e_cold(P.d, m, e) + eos_e_shear(P.d, m, e);
-            pnt += eos_p_cold(P.d, m, e) + eos_p_shear(P.d, m, e);
-            ig += eos_invG(P.d, m, e);
+            if (P.nmix) {
+                ent += eos_e_cold(P.d, m, e) + eos_e_shear(P.d, m, e);
+                pnt += eos_p_cold(P.d, m, e) + eos_p_shear(P.d, m, e);
+                ig += eos_invG(P.d, m, e);
+            } else {
+                closure_terms64(P, m, e, ent, pnt, ig);
+            }
         }
         c.p = (R)(((double)c.E + (double)c.Elo - ked - ent + pnt) / ig);
     } else {

@@ -189,6 +189,10 @@ DevParams32 make_params32(const DevParams& DP)
     DevParams32 P;
     std::memset(&P, 0, sizeof P);
     P.d = DP;
+    for (int m = 0; m < TJ_MAX_MAT; ++m) {
+        P.rG[m] = (m < DP.M && DP.prm[m][0] != 1.0) ? 1.0 / (DP.prm[m][0] - 1.0) : 0.0;
+        P.rR0h[m] = (m < DP.M && DP.prm[m][4] != 0.0) ? 0.5 / DP.prm[m][4] : 0.0;
+    }
     P.dim = DP.dim;
     P.M = DP.M;
     P.solid = DP.solid;

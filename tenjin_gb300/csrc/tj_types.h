@@ -59,6 +59,9 @@ struct DevParams32 {
     int X_ARL;
     int S_ELO;
     DevParams d;
+    // binary64 reciprocals for the closure of the binary32 cells:
+    // 1 / (prm[m][0] - 1) and 0.5 / prm[m][4]
+    double rG[TJ_MAX_MAT], rR0h[TJ_MAX_MAT];
 };
 
 // A parameter block whose material count is a compile-time constant: the
