@@ -119,12 +119,12 @@ int tj_num_cells(const tj_ctx* ctx, long long* ncells);
  * E, p, and rhomix, lambda, alphaRhoLambda, V, HenckyJ2, epsilon,
  * alphaRhoEpsilon where present); the derived ones (a, uStar, sigma, VStar,
  * devH) are recomputed on the device and not read. Download writes every
- * component of the valid cells (ghosts untouched). A page-locked buffer
- * (cudaHostAlloc / cudaHostRegister, or a pinned torch tensor) is read and
- * written in place by the conversion kernels when the device accesses host
- * memory coherently (Grace + NVLink-C2C); other buffers are staged through
- * device memory. Both give the same bytes; every call returns with the
- * transfer complete. */
+ * component of the valid cells (ghosts untouched). When the device accesses
+ * host memory coherently (Grace + NVLink-C2C), the conversion kernels read a
+ * page-locked upload buffer (cudaHostAlloc or cudaHostRegister, a pinned
+ * torch tensor) in place, and write a download buffer from cudaHostAlloc in
+ * place; other buffers are staged through device memory. Both give the same
+ * bytes; every call returns with the transfer complete. */
 int tj_upload_state(tj_ctx* ctx, int domain, int box, const double* fab, int ncomp, int ngrow);
 int tj_download_state(tj_ctx* ctx, int domain, int box, double* fab, int ncomp, int ngrow);
 /* Whole-domain exchange: ncomp blocks of nx*ny*nz doubles (valid cells, i

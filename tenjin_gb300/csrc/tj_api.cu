@@ -630,8 +630,10 @@ static int ensure_staging(tj_ctx* c, size_t bytes)
 // coherently (a Grace host over NVLink-C2C: any valid host address is legal
 // there) and both ends of the buffer are page-locked and mapped at the same
 // offset: the kernels then move each byte across the link once, at the
-// link's rate, with no staging copy and no separate conversion pass.
-static double* mapped_view(tj_ctx* c, double* host, size_t bytes)
+// link's rate, with no staging copy and no separate conversion pass. A buffer
+// the device writes must also come from cudaHostAlloc (cudaHostGetFlags
+// answers for it): registered memory may be mapped read-only to the device.
+static double* mapped_view(tj_ctx* c, double* host, size_t bytes, bool device_writes)
 {
     if (c->coherent_host < 0) {
         int dev = 0, v = 0;
@@ -648,6 +650,13 @@ static double* mapped_view(tj_ctx* c, double* host, size_t bytes)
     if (a.type != cudaMemoryTypeHost || z.type != cudaMemoryTypeHost || !a.devicePointer ||
         static_cast<const char*>(z.devicePointer) != static_cast<const char*>(a.devicePointer) + (bytes - 1))
         return nullptr;
+    if (device_writes) {
+        unsigned int flags = 0;
+        if (cudaHostGetFlags(&flags, host) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+    }
     return static_cast<double*>(a.devicePointer);
 }
 
@@ -663,7 +672,7 @@ static int exchange(tj_ctx* c, int q, const int* bx, double* host, int ncomp, in
     long long cs = (long long)ld_i * ld_j * ld_k;
     size_t bytes = sizeof(double) * ncomp * cs;
     Fp64Bufs b = bufs(c);
-    if (double* dv = mapped_view(c, host, bytes)) {
+    if (double* dv = mapped_view(c, host, bytes, !up)) {
         // in place: the kernels read (write) the caller's page-locked buffer
         if (up) {
             const DevDomain& Dq = c->doms[q];

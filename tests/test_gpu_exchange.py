@@ -85,3 +85,29 @@ def test_pinned_upload_steps_like_pageable(precision):
     np.testing.assert_array_equal(g1.state(0), g2.state(0))
     g1.close()
     g2.close()
+
+
+@pytest.mark.parametrize("precision", [FP64, MIXED])
+def test_registered_buffer_exchange(precision):
+    """Registered (cudaHostRegister) memory: read in place on upload, written
+    through the staged copy on download (registered memory may be mapped
+    read-only to the device); the same bytes as a pageable buffer."""
+    c, g = _ctx(precision)
+    ref = g.state(0)
+    buf = np.empty(ref.shape)
+    cudart = torch.cuda.cudart()
+    torch.cuda.check_error(cudart.cudaHostRegister(buf.ctypes.data, buf.nbytes, 0))
+    try:
+        g.state(0, out=buf)
+        np.testing.assert_array_equal(buf, ref)
+        buf[...] = ref
+        g.set_state(0, buf)
+        g.run(2, 1e300)
+        _, g2 = _ctx(precision)
+        g2.set_state(0, ref.copy())
+        g2.run(2, 1e300)
+        np.testing.assert_array_equal(g.state(0), g2.state(0))
+        g2.close()
+    finally:
+        torch.cuda.check_error(cudart.cudaHostUnregister(buf.ctypes.data))
+    g.close()
