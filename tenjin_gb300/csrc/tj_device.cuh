@@ -563,7 +563,7 @@ __device__ inline int mix_root_find(const PD& P, CellT<double>& c, double ke)
 // curve: three, against three and eight); other EOS go through the general
 // functions.
 template <typename P32>
-__device__ inline void closure_terms64(const P32& P, int m, const ECellT<double>& e, double& ent, double& pnt,
+__device__ __forceinline__ void closure_terms64(const P32& P, int m, const ECellT<double>& e, double& ent, double& pnt,
                                        double& ig)
 {
     const double* q = P.d.prm[m];
@@ -595,7 +595,7 @@ __device__ inline void closure_terms64(const P32& P, int m, const ECellT<double>
 // conservativeToPrimitive (:67-122). Returns 0, or TJ_ERR_ROOT from the
 // mixture closure.
 template <typename PT>
-__device__ inline int c2p(const PT& P, CellT<typename PT::real>& c)
+__device__ __forceinline__ int c2p(const PT& P, CellT<typename PT::real>& c)
 {
     using R = typename PT::real;
     int err = 0;
