@@ -15,8 +15,9 @@ keys the reference reads onto a :class:`~tenjin_gb300.cases.Case`:
   adiabaticIndex, pref, eref, CV, then rho0 K0 EOSalpha EOSbeta (Romenskii) or
   rho0 e1..e5 (Wilkins), G0 for solids, yieldStress when PLASTIC; a fluid with
   mixture = 1 is a MixtureEOS with adiabaticIndexmix, prefmix, erefmix, CVmix;
-* listOfStates (getState, initialise.cpp:237-267): per material alpha, rho,
-  lambda (the mixture) and F[9] (solids), then p, u, v, w.
+* listOfStates (getState, initialise.cpp:237-267): per material alpha, then
+  rho (fluids), rhoa and lambda (the mixture) or F[9] (solids); then p, u, v,
+  w.
 
 The reference chooses the state of each cell with a hard-coded geometry
 (chooseStateBasedOnInitialCondition, initialise.cpp:387-): ``to_case`` takes
@@ -215,7 +216,12 @@ def to_case(cfg: Dict[str, Any], dim: int, max_grid_size: int,
         for m in range(M):
             sm = st["material"][m]
             prim[m][msk] = float(sm["alpha"])
-            rho = float(sm["rho"])
+            # getState (initialise.cpp:242-257): a mixture's density is
+            # "rhoa", a fluid's "rho"; a solid's comes from F
+            if mats[m].eos == cases.EOS_MIXTURE:
+                rho = float(sm["rhoa"])
+            elif mats[m].phase != cases.PHASE_SOLID:
+                rho = float(sm["rho"])
             if mats[m].phase == cases.PHASE_SOLID:
                 F = [float(v) for v in sm.get("F", [1, 0, 0, 0, 1, 0, 0, 0, 1])]
                 Fm = np.array(F).reshape(3, 3)

@@ -76,7 +76,9 @@ def test_to_case_maps_a_mixture_and_reactive():
     m0["mixture"] = 1
     m0.update({"adiabaticIndexmix": 1.4, "prefmix": 0.0, "erefmix": 0.0, "CVmix": 1000.0})
     for st, lam in zip(cfg["listOfStates"], (0.7, 0.999)):
+        # a mixture's state names its density rhoa (initialise.cpp:245-248)
         st["material"][0]["lambda"] = lam
+        st["material"][0]["rhoa"] = st["material"][0].pop("rho")
     c = settings.to_case(cfg, 1, 50)
     assert c.nmix == 1 and c.reactive == 1
     assert c.materials[0].eos == cases.EOS_MIXTURE
@@ -85,6 +87,7 @@ def test_to_case_maps_a_mixture_and_reactive():
     assert d.prim.shape[0] == c.nprim
     assert np.all(d.prim[-1, 0, 0, :50] == 0.7) and np.all(d.prim[-1, 0, 0, 50:] == 0.999)
     # initialise.cpp:104 with rhomix = rho_k: p += sum p_cold / sum alpha/Gamma
+    assert np.all(d.prim[2, 0, 0, :50] == 1000.0) and np.all(d.prim[3, 0, 0, :50] == 1.2)
     a0, lam = 0.999999, 0.7
     g = (lam * 4.4 * 1.0 + (1 - lam) * 1.4 * 1000.0) / (lam * 1.0 + (1 - lam) * 1000.0) - 1.0
     pc = (-2.64e9 * a0 / 3.4) * lam
