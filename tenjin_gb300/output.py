@@ -14,8 +14,10 @@
   ``<dir>/<var><picture, 2 digits>`` with one ``i value`` line per cell,
   boxes in box-list order.
 
-``read_plotfile`` reads such a plotfile back (used by the tests, and handy to
-compare a GPU run with the reference's own plotfiles).
+``PictureSchedule`` says after which steps the reference writes a plotfile
+(numberOfPictures over finalTime). ``read_plotfile`` reads such a plotfile
+back (used by the tests, and handy to compare a GPU run with the reference's
+own plotfiles).
 """
 from __future__ import annotations
 
@@ -157,6 +159,37 @@ def write_plotfile(path: str, case: Case, state: np.ndarray, time: float, step: 
                 f.write(f"{lo[k] * dx[k]:.17g} {(hi[k] + 1) * dx[k]:.17g}\n")
         f.write("Level_0/Cell\n")
     return path
+
+
+class PictureSchedule:
+    """The reference's plotfile cadence (main.cpp:119-180). Its time loop is
+    ``for (t = 0; t < finalT; t += dt, n++)``; after the update of each step it
+    writes a plotfile of the new state, named and stamped with that step's
+    loop values (t, n) -- the time and index at the START of the step -- when
+    ``t > counter * finalT / numberOfPictures``, and then advances the counter
+    (from 0). Step 0's initial state and the final state (stamped finalT and
+    the final n) are always written (main.cpp:104-106, 196-199).
+
+    ``due(t)`` is that test for the step that started at time t; call it once
+    per step, in order."""
+
+    def __init__(self, final_t: float, pictures: int):
+        if pictures <= 0:
+            raise ValueError("numberOfPictures must be positive")
+        self.final_t = float(final_t)
+        self.pictures = int(pictures)
+        self.counter = 0
+
+    @classmethod
+    def from_settings(cls, cfg: Dict[str, object]) -> "PictureSchedule":
+        """finalTime and numberOfPictures of a parsed settings file."""
+        return cls(float(cfg["finalTime"]), int(cfg["numberOfPictures"]))
+
+    def due(self, t: float) -> bool:
+        if t > float(self.counter) * self.final_t / float(self.pictures):
+            self.counter += 1
+            return True
+        return False
 
 
 def plotfile_name(filename: str, step: int) -> str:

@@ -2,6 +2,7 @@
 import os
 
 import numpy as np
+import pytest
 
 from tenjin_gb300 import cases, output
 
@@ -57,3 +58,27 @@ def test_gnuplot_dump(tmp_path):
     vals = {int(l.split()[0]): float(l.split()[1]) for l in lines}
     assert sorted(vals) == list(range(40))
     assert vals[5] == float(f"{st[3 * c.M, 0, 0, 5]:g}")
+
+
+def test_picture_schedule_follows_the_reference_loop():
+    # main.cpp:121-180 with exact binary steps: finalT 1, 4 pictures, dt 1/8;
+    # the test t > counter * finalT / pictures fires at the steps that start
+    # at t = 1/8, 3/8, 5/8, 7/8 (n = 1, 3, 5, 7)
+    sch = output.PictureSchedule(1.0, 4)
+    t, n, written = 0.0, 0, []
+    while t < 1.0:
+        if sch.due(t):
+            written.append(n)
+        t += 0.125
+        n += 1
+    assert written == [1, 3, 5, 7] and sch.counter == 4
+    with pytest.raises(ValueError):
+        output.PictureSchedule(1.0, 0)
+
+
+def test_picture_schedule_from_settings():
+    from tenjin_gb300 import settings
+    cfg = settings.parse("finalTime = 0.2; numberOfPictures = 10;")
+    sch = output.PictureSchedule.from_settings(cfg)
+    assert sch.final_t == 0.2 and sch.pictures == 10
+    assert not sch.due(0.0) and sch.due(1e-9) and not sch.due(0.02) and sch.due(0.0200001)
