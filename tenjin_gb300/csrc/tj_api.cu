@@ -672,12 +672,14 @@ static int exchange(tj_ctx* c, int q, const int* bx, double* host, int ncomp, in
     long long cs = (long long)ld_i * ld_j * ld_k;
     size_t bytes = sizeof(double) * ncomp * cs;
     Fp64Bufs b = bufs(c);
+    // an upload of the whole of the only domain replaces the state entirely;
+    // any other keeps the cells outside the box
+    const DevDomain& Dq = c->doms[q];
+    const bool whole = c->doms.size() == 1 && bx[0] == 0 && bx[1] == 0 && bx[2] == 0 && bx[3] == Dq.n[0] - 1 &&
+                       bx[4] == Dq.n[1] - 1 && bx[5] == Dq.n[2] - 1;
     if (double* dv = mapped_view(c, host, bytes, !up)) {
         // in place: the kernels read (write) the caller's page-locked buffer
         if (up) {
-            const DevDomain& Dq = c->doms[q];
-            const bool whole = c->doms.size() == 1 && bx[0] == 0 && bx[1] == 0 && bx[2] == 0 &&
-                               bx[3] == Dq.n[0] - 1 && bx[4] == Dq.n[1] - 1 && bx[5] == Dq.n[2] - 1;
             if (!whole) a_sync(c);
             // the fused 2-D state is filled in the same pass (no conversion
             // before the next step)
@@ -700,11 +702,6 @@ static int exchange(tj_ctx* c, int q, const int* bx, double* host, int ncomp, in
     e = ensure_staging(c, bytes);
     if (e) return e;
     if (up) {
-        // the cells outside this box keep their current values; a box that is
-        // the whole of the only domain replaces the state entirely
-        const DevDomain& Dq = c->doms[q];
-        const bool whole = c->doms.size() == 1 && bx[0] == 0 && bx[1] == 0 && bx[2] == 0 && bx[3] == Dq.n[0] - 1 &&
-                           bx[4] == Dq.n[1] - 1 && bx[5] == Dq.n[2] - 1;
         if (!whole) a_sync(c);
         // only the component planes the carried state is built from cross the
         // link (k_ap_to_state reads no other)
