@@ -53,6 +53,12 @@ FIXTURES = {
                                                    "reactive": 0, "reactant": [2.5, 0.0, 4.0e6, 1500.0]}),
     "reactive_spherical_1d": ("reactive_charge", {"dim": 1, "n": 160, "max_grid_size": 40, "max_steps": 100},
                               {"radial": 1, "lo_bc": [1, 0, 0]}),
+    # domains and boxes narrower than the stencils (2 ghost cells, the THINC
+    # candidate's neighbours and the Youngs normal)
+    "sod3_tiny": ("sod_1d", {"ncells": 3, "max_grid_size": 3, "max_steps": 6}),
+    "bubble3_tiny": ("shock_bubble_2d", {"n": 3, "max_grid_size": 3, "max_steps": 6, "radius": 0.3}),
+    "bubble4_reflect_boxes2": ("shock_bubble_2d", {"n": 4, "max_grid_size": 2, "max_steps": 6, "radius": 0.3},
+                               {"lo_bc": [1, 1, 0], "hi_bc": [1, 1, 0]}),
 }
 
 
