@@ -559,8 +559,8 @@ __device__ inline int mix_root_find(const PD& P, CellT<double>& c, double ke)
 // material for the binary64 pressure closure of a binary32 cell: the
 // formulas of eos_e_cold + eos_e_shear, eos_p_cold + eos_p_shear and
 // eos_invG, with each quotient formed once and the constant ones taken from
-// the precomputed reciprocals (a stiffened gas: one division, the Hugoniot
-// curve: three, against three and eight); other EOS go through the general
+// the precomputed reciprocals (a stiffened gas: no division instead of two,
+// the Hugoniot curve: two instead of eight); other EOS go through the general
 // functions.
 template <typename P32>
 __device__ __forceinline__ void closure_terms64(const P32& P, int m, const ECellT<double>& e, double& ent, double& pnt,
