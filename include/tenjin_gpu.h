@@ -233,12 +233,15 @@ int tj_backward(tj_ctx* ctx, int domain, const double* grad_state, double* grad_
  * buffers its host hands it, a running loop that must not allocate). Needs no
  * context. state: DEVICE pointer to one domain's state in the AccessPattern
  * layout (tj_ncomp blocks of nx*ny*nz doubles, i fastest); dt: HOST pointer
- * receiving CFL * min(dx/(a+|u|)) as tj_compute_dt computes it; stream: the
- * cudaStream_t to order the work on (NULL: the default stream). Working
- * memory is a fixed array inside the library (TJ_NOALLOC_MAX_CELLS bounds the
- * domain; larger domains return TJ_ERR_ARG). The first call on a device looks
- * up that array's address; make it before any stream capture. Calls that
- * overlap on the GPU share the array and race: serialise them. */
+ * receiving CFL * min(dx/(a+|u|)) computed in binary64, as tj_compute_dt
+ * computes it for a TJ_PRECISION_FP64 context (params->precision is not
+ * read); stream: the cudaStream_t to order the work on (NULL: the default
+ * stream). Working memory is a fixed array inside the library
+ * (TJ_NOALLOC_MAX_CELLS bounds the domain; larger domains return
+ * TJ_ERR_ARG). The first call on a device looks up that array's address.
+ * Every call copies dt to the host and synchronises the stream, so no call
+ * may be made while that stream is being captured. Calls that overlap on the
+ * GPU share the array and race: serialise them. */
 #define TJ_NOALLOC_MAX_CELLS (1 << 24)
 int tj_compute_dt_noalloc(const tj_params* params, const int* n_cells, const double* dim_l, const double* state,
                           double* dt, void* stream);

@@ -22,12 +22,15 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REF_DIR = os.path.join(HERE, "_ref")
 
 
-def ref_binary(dim: int, omp: bool = False) -> str:
-    return os.path.join(REF_DIR, f"tenjin_ref_{'omp_' if omp else ''}{dim}d")
+def ref_binary(dim: int, omp: bool = False, stock: bool = False) -> str:
+    """Path of a reference binary: serial with the pinned libm (parity),
+    OpenMP (timing), or serial against the host's own libm (stock)."""
+    kind = "omp_" if omp else "stock_" if stock else ""
+    return os.path.join(REF_DIR, f"tenjin_ref_{kind}{dim}d")
 
 
-def have_ref(dim: int = 1) -> bool:
-    return os.path.exists(ref_binary(dim))
+def have_ref(dim: int = 1, stock: bool = False) -> bool:
+    return os.path.exists(ref_binary(dim, stock=stock))
 
 
 def write_input(case, path: str) -> None:
@@ -79,8 +82,9 @@ def read_output(case, path: str):
     return {"t": t, "dts": dts, "nan_stop": bool(nan_stop), "ncomp": ncomp, "elapsed": elapsed, "states": states}
 
 
-def run_reference(case, omp: bool = False, threads: int | None = None, timeout: float = 3600.0):
-    exe = ref_binary(case.dim, omp)
+def run_reference(case, omp: bool = False, threads: int | None = None, timeout: float = 3600.0,
+                  stock: bool = False):
+    exe = ref_binary(case.dim, omp, stock)
     if not os.path.exists(exe):
         raise FileNotFoundError(f"{exe} missing: build it with `make -C oracle` where the reference tree exists")
     with tempfile.TemporaryDirectory() as td:

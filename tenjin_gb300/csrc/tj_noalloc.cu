@@ -25,6 +25,14 @@
 // Set-up: the first call on a device looks up the array's device address
 // with cudaGetSymbolAddress, with that device current, and caches it. Make
 // that first call before any stream capture begins.
+//
+// Every call copies dt into host memory and synchronises the stream, so no
+// call may be made while that stream is being captured into a graph.
+//
+// The arithmetic is binary64 whatever the precision field of the parameters
+// says: dt is the one tj_compute_dt gives for a TJ_PRECISION_FP64 context on
+// the same state (a context that carries binary32 state computes its own dt
+// from that state, which differs by rounding).
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -32,6 +40,7 @@
 #include <mutex>
 
 #include "tj_device.cuh"
+#include "tj_layout.h"
 #include "tj_types.h"
 
 namespace tj {
@@ -144,51 +153,49 @@ extern "C" int tj_compute_dt_noalloc(const tj_params* p, const int* n_cells, con
         std::fprintf(stderr, "tj_compute_dt_noalloc: unsupported parameters\n");
         return TJ_ERR_ARG;
     }
+    // The same component offsets as the context's (AccessPattern order).
+    DevParams P;
+    make_layouts(*p, P);
     NaLayout L;
-    L.M = p->n_materials;
-    L.dim = p->dim;
-    L.solid = p->SOLID;
-    L.cfl = p->CFL;
+    L.M = P.M;
+    L.dim = P.dim;
+    L.solid = P.solid;
+    L.cfl = P.cfl;
     L.N = 1;
     for (int d = 0; d < 3; ++d) {
         L.n[d] = d < p->dim ? n_cells[d] : 1;
-        if (L.n[d] < 1) return TJ_ERR_ARG;
+        // each extent and the running product stay within the maximum, so the
+        // product never overflows
+        if (L.n[d] < 1 || L.n[d] > TJ_NOALLOC_MAX_CELLS || L.N * L.n[d] > TJ_NOALLOC_MAX_CELLS) {
+            std::fprintf(stderr,
+                         "tj_compute_dt_noalloc: domain extent %d along axis %d is not positive or exceeds the maximum "
+                         "of %d cells (TJ_NOALLOC_MAX_CELLS)\n",
+                         L.n[d], d, TJ_NOALLOC_MAX_CELLS);
+            return TJ_ERR_ARG;
+        }
         L.dx[d] = (d < p->dim ? dim_l[d] : 1.0) / (double)L.n[d];
         L.N *= L.n[d];
     }
-    if (L.N > TJ_NOALLOC_MAX_CELLS) {
-        std::fprintf(stderr, "tj_compute_dt_noalloc: %lld cells exceed the maximum of %d (TJ_NOALLOC_MAX_CELLS)\n", L.N,
-                     TJ_NOALLOC_MAX_CELLS);
-        return TJ_ERR_ARG;
-    }
-    // AccessPattern offsets (accesspattern.cpp:44-79)
-    const int M = L.M;
-    L.A_ALPHA = 0;
-    L.A_ARHO = M;
-    L.A_RHOK = 2 * M;
-    L.A_RHO = 3 * M;
-    L.A_VEL = 3 * M + 4;
-    L.A_P = 3 * M + 8;
-    L.A_HJ2 = 3 * M + 11 + 9 + 27;
-    DevParams P;
-    std::memset(&P, 0, sizeof P);
-    P.dim = p->dim;
-    P.M = M;
-    P.solid = p->SOLID;
-    for (int m = 0; m < M; ++m) {
-        P.phase[m] = p->materials[m].phase;
-        P.eos[m] = p->materials[m].eos;
-        for (int q = 0; q < TJ_MAX_EOS_PARAMS; ++q)
-            P.prm[m][q] = q < p->materials[m].nparams ? p->materials[m].params[q] : 0.0;
-        if (P.phase[m] == TJ_PHASE_SOLID) P.any_solid = 1;
-    }
+    L.A_ALPHA = P.A_ALPHA;
+    L.A_ARHO = P.A_ARHO;
+    L.A_RHOK = P.A_RHOK;
+    L.A_RHO = P.A_RHO;
+    L.A_VEL = P.A_VEL;
+    L.A_P = P.A_P;
+    L.A_HJ2 = P.A_HJ2;
     double* scratch = scratch_for_current_device();
     if (!scratch) return TJ_ERR_CUDA;
     cudaStream_t st = (cudaStream_t)stream;
-    const int nb = (int)((L.N + kNaCellsPerBlock - 1) / kNaCellsPerBlock);
-    k_na_cfl_partial<<<nb, kNaThreads, 0, st>>>(P, L, state, scratch);
-    k_na_cfl_final<<<1, kNaThreads, 0, st>>>(nb, L.cfl, scratch);
-    if (cudaGetLastError() != cudaSuccess) return TJ_ERR_CUDA;
+    int nb = (int)((L.N + kNaCellsPerBlock - 1) / kNaCellsPerBlock);
+    double cfl = L.cfl;
+    // cudaLaunchKernel reports this launch's own failure, and leaves any error
+    // that earlier, unrelated work left pending to its owner
+    void* a1[] = {&P, &L, &state, &scratch};
+    if (cudaLaunchKernel((const void*)k_na_cfl_partial, dim3(nb), dim3(kNaThreads), a1, 0, st) != cudaSuccess)
+        return TJ_ERR_CUDA;
+    void* a2[] = {&nb, &cfl, &scratch};
+    if (cudaLaunchKernel((const void*)k_na_cfl_final, dim3(1), dim3(kNaThreads), a2, 0, st) != cudaSuccess)
+        return TJ_ERR_CUDA;
     if (cudaMemcpyAsync(dt, scratch + kNaMaxBlocks, sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess)
         return TJ_ERR_CUDA;
     if (cudaStreamSynchronize(st) != cudaSuccess) return TJ_ERR_CUDA;

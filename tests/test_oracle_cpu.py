@@ -80,3 +80,25 @@ def test_port_matches_live_reference_random_inputs():
     p = port.run_port(c)
     np.testing.assert_array_equal(r["dts"], p["dts"])
     assert fx.exact_fraction(p["states"][0], r["states"][0]) == 1.0
+
+
+# Fixtures whose arithmetic needs no transcendental result whose last bit
+# matters (no THINC jump, no pow/log in the EOS along their trajectory): the
+# reference linked against the host's own libm reproduces them bit for bit, so
+# the project-written exp/cosh/tanh/pow/log that both sides use for parity do
+# not decide these results.
+STOCK_EXACT = ["bubble32_muscl", "bubble3_tiny", "bubble4_reflect_boxes2", "copper12", "fluid3d_boxes",
+               "hugoniot2d_plastic", "mixture_closed_form_2d", "sod1000_full", "sod200_boxes", "sod3_tiny",
+               "sod_spherical_1d", "uneven3d_4dom", "wilkins2d_plastic_cylindrical"]
+
+
+@pytest.mark.skipif(not refio.have_ref(3, stock=True),
+                    reason="the stock-libm reference binaries are built only where the reference tree exists")
+@pytest.mark.parametrize("name", STOCK_EXACT)
+def test_stock_libm_reference_reproduces_fixture(name):
+    c = fx.build_case(name)
+    gold = fx.load(name)
+    r = refio.run_reference(c, stock=True)
+    np.testing.assert_array_equal(r["dts"], gold["dts"])
+    for q, st in enumerate(r["states"]):
+        assert fx.exact_fraction(st[gold["carried"]], gold["states"][q]) == 1.0
