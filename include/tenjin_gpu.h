@@ -173,6 +173,19 @@ int tj_prim_to_cons(tj_ctx* ctx);
 /* CellArray::contains_nan (cellarray.cpp:101-116): *flag = 1 if NaN. */
 int tj_contains_nan(tj_ctx* ctx, int* flag);
 
+/* Global conservation sums of the current state in binary64: sums[k] for
+ * k < n_materials is the sum over the valid cells of every domain of
+ * alphaRho_k * cell volume, sums[n_materials + r] (r = 0, 1, 2) that of rhoU_r,
+ * sums[n_materials + 3] that of E. The reduction order is fixed, so the same
+ * state gives the same bits on any GPU. HOST array of n_materials + 4 doubles.
+ * No reference counterpart (the reference checks only for NaN,
+ * cellarray.cpp:101-116). */
+int tj_conservation_sums(tj_ctx* ctx, double* sums);
+/* One AccessPattern component (accesspattern.cpp:44-79) of one domain's valid
+ * cells, nx*ny*nz doubles, i fastest: the plane tj_download_domain writes at
+ * that component, without moving the others. */
+int tj_download_component(tj_ctx* ctx, int domain, int comp, double* data);
+
 /* One iteration of the time loop of main.cpp:121-191 with dt and t kept on
  * the device: dt = getTimeStep, clamped to t_end, times 0.2 for the first
  * five steps; advance; reactiveUpdate (REACTIVE); plasticUpdate (PLASTIC);

@@ -35,9 +35,11 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <fstream>
 #include <iostream>
 #include <limits>
 #include <map>
+#include <sstream>
 #include <string>
 #include <vector>
 #ifdef _OPENMP
@@ -71,6 +73,38 @@ template <class T, std::size_t N>
 using Array = std::array<T, N>;
 
 inline std::ostream& Print() { return std::cout; }
+
+// AllPrintToFile(name) << ...: the text is collected in a string stream with
+// the stream's default precision (6 significant digits) and appended to the
+// file when the statement ends. AMReX's own class is version-dependent (some
+// versions suffix the file name with the rank); one serial process here
+// appends to the name as given.
+class PrintToFile {
+public:
+    explicit PrintToFile(std::string name) : name_(std::move(name)) {}
+    ~PrintToFile()
+    {
+        std::ofstream f(name_, std::ios_base::app);
+        f << ss_.str();
+    }
+    template <class T>
+    PrintToFile& operator<<(const T& v)
+    {
+        ss_ << v;
+        return *this;
+    }
+    PrintToFile& operator<<(std::ostream& (*m)(std::ostream&))
+    {
+        ss_ << m;
+        return *this;
+    }
+
+private:
+    std::string name_;
+    std::ostringstream ss_;
+};
+
+using AllPrintToFile = PrintToFile;
 
 inline double second()
 {

@@ -124,7 +124,7 @@ struct Sim {
 
 int main(int argc, char** argv)
 {
-    if (argc < 3) { std::fprintf(stderr, "usage: %s in.bin out.bin\n", argv[0]); return 2; }
+    if (argc < 3) { std::fprintf(stderr, "usage: %s in.bin out.bin [gnuplot-dir]\n", argv[0]); return 2; }
 
     Reader rd(argv[1]);
     if (rd.i32() != 0x544a4f52) { std::fprintf(stderr, "bad magic\n"); return 2; }
@@ -308,6 +308,9 @@ int main(int argc, char** argv)
         if (nan_stop) break;
     }
     double elapsed = amrex::second() - t0;
+    // optional: the reference's 1-D gnuplot dump of the final state of the
+    // first domain (print.cpp:33-43), picture 0, into the directory argv[3]
+    if (argc > 3) PrintAllVarsTo1DGnuplotFile(*sims[0].U1, 0, std::string(argv[3]));
 
     std::ofstream out(argv[2], std::ios::binary);
     int32_t hdr[4] = {0x544a4f55, (int32_t)dts.size(), nan_stop ? 1 : 0, sims[0].parameters.Ncomp};

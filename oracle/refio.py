@@ -83,7 +83,10 @@ def read_output(case, path: str):
 
 
 def run_reference(case, omp: bool = False, threads: int | None = None, timeout: float = 3600.0,
-                  stock: bool = False):
+                  stock: bool = False, gnuplot_dir: str | None = None):
+    """Run the reference binary on `case`. With gnuplot_dir, the reference's
+    PrintAllVarsTo1DGnuplotFile (print.cpp:33-43) also writes its 1-D dump of
+    the first domain's final state there (picture 0)."""
     exe = ref_binary(case.dim, omp, stock)
     if not os.path.exists(exe):
         raise FileNotFoundError(f"{exe} missing: build it with `make -C oracle` where the reference tree exists")
@@ -93,7 +96,8 @@ def run_reference(case, omp: bool = False, threads: int | None = None, timeout: 
         env = dict(os.environ)
         if threads is not None:
             env["OMP_NUM_THREADS"] = str(threads)
-        r = subprocess.run([exe, fin, fout], capture_output=True, text=True, timeout=timeout, env=env)
+        argv = [exe, fin, fout] + ([gnuplot_dir] if gnuplot_dir else [])
+        r = subprocess.run(argv, capture_output=True, text=True, timeout=timeout, env=env)
         if r.returncode != 0:
             raise RuntimeError(f"reference run failed ({r.returncode}): {r.stdout[-2000:]} {r.stderr[-2000:]}")
         out = read_output(case, fout)

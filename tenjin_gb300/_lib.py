@@ -71,6 +71,8 @@ SIGNATURES = [
     ("tj_cons_to_prim", _I, [_P]),
     ("tj_prim_to_cons", _I, [_P]),
     ("tj_contains_nan", _I, [_P, _PI]),
+    ("tj_conservation_sums", _I, [_P, _PD]),
+    ("tj_download_component", _I, [_P, _I, _I, _PD]),
     ("tj_step", _I, [_P, _D]),
     ("tj_run", _I, [_P, _I, _D, _PI, _PD]),
     ("tj_get_time", _I, [_P, _PD, _PI, _PD]),

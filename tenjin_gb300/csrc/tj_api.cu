@@ -133,6 +133,7 @@ struct tj_ctx {
     EventProf* prof = nullptr;
     long long graph_launches = 0;
     AdjState* adj = nullptr;  // checkpoints and buffers of tj_forward / tj_backward
+    double* cons = nullptr;   // conservation sums: partials, then the M + 4 results
 };
 
 namespace {
@@ -395,6 +396,7 @@ int tj_destroy(tj_ctx* c)
     delete c->prof;
     c->prof = nullptr;
     if (c->d_scal) cudaFree(c->d_scal);
+    if (c->cons) cudaFree(c->cons);
     for (cudaEvent_t& e : c->slab_ev)
         if (e) cudaEventDestroy(e);
     if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
@@ -828,6 +830,46 @@ int tj_contains_nan(tj_ctx* c, int* flag)
     TJ_CUDA(c, cudaStreamSynchronize(c->stream));
     TJ_CUDA(c, cudaMemsetAsync(&c->d_scal->nan_flag, 0, sizeof(int), c->stream));
     *flag = s.nan_flag ? 1 : 0;
+    return TJ_OK;
+}
+
+int tj_conservation_sums(tj_ctx* c, double* sums)
+{
+    if (!c || !sums) return TJ_ERR_ARG;
+    int e = need_state(c);
+    if (e) return e;
+    const int nv = c->P.M + 4;
+    if (!c->cons) TJ_CUDA(c, cudaMalloc(&c->cons, sizeof(double) * (size_t)(kConsPartials + 1) * nv));
+    a_sync(c);
+    Fp64Bufs b = bufs(c);
+    double* out = c->cons + (size_t)kConsPartials * nv;
+    c->launches += fp64_conservation(c->P, b, c->A, c->cons, out, c->stream);
+    TJ_CUDA(c, cudaMemcpyAsync(sums, out, sizeof(double) * nv, cudaMemcpyDeviceToHost, c->stream));
+    TJ_CUDA(c, cudaStreamSynchronize(c->stream));
+    TJ_CUDA(c, cudaGetLastError());
+    return TJ_OK;
+}
+
+int tj_download_component(tj_ctx* c, int q, int comp, double* data)
+{
+    if (!c || q < 0 || q >= (int)c->doms.size() || !data || comp < 0 || comp >= c->P.NCOMP)
+        return fail(c, TJ_ERR_ARG, "bad component download arguments");
+    int e = need_state(c);
+    if (e) return e;
+    const DevDomain& D = c->doms[q];
+    const size_t bytes = sizeof(double) * (size_t)D.n[0] * D.n[1] * D.n[2];
+    double* dst = mapped_view(c, data, bytes, true);
+    if (!dst) {
+        e = ensure_staging(c, bytes);
+        if (e) return e;
+        dst = c->staging;
+    }
+    a_sync(c);
+    Fp64Bufs b = bufs(c);
+    c->launches += fp64_state_component(c->P, b, q, c->A, comp, dst, c->stream);
+    if (dst == c->staging) TJ_CUDA(c, cudaMemcpyAsync(data, dst, bytes, cudaMemcpyDeviceToHost, c->stream));
+    TJ_CUDA(c, cudaStreamSynchronize(c->stream));
+    TJ_CUDA(c, cudaGetLastError());
     return TJ_OK;
 }
 

@@ -257,6 +257,106 @@ __global__ void k_prim_to_state(DevParams P, Fp64Bufs b, int dom, const double* 
 }
 
 // ---------------------------------------------------------------------------
+// Global conservation sums in binary64: per cell alphaRho_k, rhoU and E times
+// the cell volume, summed over the valid cells of every domain. The partition
+// is fixed (kConsBlocks blocks of contiguous cell ranges, each thread a fixed
+// stride, a fixed tree per block and over the blocks), so the result does
+// not depend on the GPU or on scheduling: the same state gives the same bits.
+// ---------------------------------------------------------------------------
+static constexpr int kConsBlocks = kConsPartials;
+
+__global__ void __launch_bounds__(kThreads) k_cons_partial(DevParams P, Fp64Bufs b, const double* X, double* part)
+{
+    const long long nt = b.ntot;
+    const int nv = P.M + 4;
+    const long long chunk = (nt + kConsBlocks - 1) / kConsBlocks;
+    const long long g0 = blockIdx.x * chunk, g1 = min(nt, g0 + chunk);
+    double acc[TJ_MAX_MAT + 4];
+    for (int v = 0; v < TJ_MAX_MAT + 4; ++v) acc[v] = 0.0;
+    int q = -1;
+    long long qlo = 0, qhi = -1;  // cell range of domain q
+    for (long long g = g0 + threadIdx.x; g < g1; g += kThreads) {
+        if (g < qlo || g >= qhi) {
+            q = find_dom(b.doms, b.ndom, g);
+            qlo = b.doms[q].off;
+            qhi = qlo + (long long)b.doms[q].n[0] * b.doms[q].n[1] * b.doms[q].n[2];
+        }
+        const DevDomain& D = b.doms[q];
+        const double dv = D.dx[0] * (P.dim > 1 ? D.dx[1] : 1.0) * (P.dim > 2 ? D.dx[2] : 1.0);
+        for (int m = 0; m < P.M; ++m) acc[m] += X[(P.S_ARHO + m) * nt + g] * dv;
+        for (int r = 0; r < 3; ++r) acc[P.M + r] += X[(P.S_RHOU + r) * nt + g] * dv;
+        acc[P.M + 3] += X[P.S_E * nt + g] * dv;
+    }
+    __shared__ double red[kThreads];
+    for (int v = 0; v < nv; ++v) {
+        red[threadIdx.x] = acc[v];
+        __syncthreads();
+        for (int h = kThreads / 2; h > 0; h >>= 1) {
+            if ((int)threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) part[(long long)v * kConsBlocks + blockIdx.x] = red[0];
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(kConsBlocks) k_cons_final(int nv, const double* part, double* out)
+{
+    __shared__ double red[kConsBlocks];
+    for (int v = 0; v < nv; ++v) {
+        red[threadIdx.x] = part[(long long)v * kConsBlocks + threadIdx.x];
+        __syncthreads();
+        for (int h = kConsBlocks / 2; h > 0; h >>= 1) {
+            if ((int)threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) out[v] = red[0];
+        __syncthreads();
+    }
+}
+
+// One AccessPattern component of one domain's valid cells (i fastest), with
+// the derived components computed as in k_state_to_ap.
+__global__ void k_state_component(DevParams P, Fp64Bufs b, int dom, const double* X, int comp, double* out)
+{
+    const long long nt = b.ntot;
+    const DevDomain D = b.doms[dom];
+    const long long nd = (long long)D.n[0] * D.n[1] * D.n[2];
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nd; t += (long long)gridDim.x * blockDim.x) {
+        CellS c;
+        load_state(P, X, nt, D.off + t, nullptr, c);
+        // the derived components in k_state_to_ap's order
+        const double hj2 = c.hj2;
+        if (P.solid) hencky(P, c);
+        c.hj2 = hj2;
+        stress(P, c);
+        double v = 0.0;
+        const auto in = [](int cmp, int first, int n) { return first >= 0 && cmp >= first && cmp < first + n; };
+        if (in(comp, P.A_ALPHA, P.M)) v = c.alpha[comp - P.A_ALPHA];
+        else if (in(comp, P.A_ARHO, P.M)) v = c.arho[comp - P.A_ARHO];
+        else if (in(comp, P.A_RHOK, P.M)) v = c.rhok[comp - P.A_RHOK];
+        else if (comp == P.A_RHO) v = c.rho;
+        else if (in(comp, P.A_RHOU, 3)) v = c.rhou[comp - P.A_RHOU];
+        else if (in(comp, P.A_VEL, 3)) v = c.vel[comp - P.A_VEL];
+        else if (comp == P.A_E) v = c.E;
+        else if (comp == P.A_P) v = c.p;
+        else if (comp == P.A_A) v = sound_speed(P, c);
+        else if (comp == P.A_USTAR || in(comp, P.A_VSTAR, 9)) v = 0.0;
+        else if (in(comp, P.A_SIGMA, 9)) v = c.sigma[comp - P.A_SIGMA];
+        else if (in(comp, P.A_DEVH, 9)) v = c.devH[comp - P.A_DEVH];
+        else if (in(comp, P.A_V, 9)) v = c.V[comp - P.A_V];
+        else if (comp == P.A_HJ2) v = c.hj2;
+        else if (in(comp, P.A_EPS, P.M)) v = c.eps[comp - P.A_EPS];
+        else if (in(comp, P.A_ARE, P.M)) v = c.are[comp - P.A_ARE];
+        else if (comp == P.A_RMIX) v = c.rm0;
+        else if (P.A_RMIX >= 0 && comp == P.A_RMIX + 1) v = c.rm1;
+        else if (comp == P.A_LAM) v = c.lam;
+        else if (comp == P.A_ARL) v = c.arl;
+        out[t] = v;
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Host launchers.
 // ---------------------------------------------------------------------------
 #define PROF_BEGIN(name) \
@@ -325,6 +425,20 @@ int fp64_state_to_ap(const DevParams& P, const Fp64Bufs& b, int dom, const int* 
 int fp64_prim_to_state(const DevParams& P, const Fp64Bufs& b, int dom, const double* prim, double* X, cudaStream_t st)
 {
     k_prim_to_state<<<nblocks(b.ntot), kThreads, 0, st>>>(P, b, dom, prim, X);
+    return 1;
+}
+
+int fp64_conservation(const DevParams& P, const Fp64Bufs& b, const double* X, double* part, double* out, cudaStream_t st)
+{
+    k_cons_partial<<<kConsBlocks, kThreads, 0, st>>>(P, b, X, part);
+    k_cons_final<<<1, kConsBlocks, 0, st>>>(P.M + 4, part, out);
+    return 2;
+}
+
+int fp64_state_component(const DevParams& P, const Fp64Bufs& b, int dom, const double* X, int comp, double* out,
+                         cudaStream_t st)
+{
+    k_state_component<<<nblocks(b.ntot), kThreads, 0, st>>>(P, b, dom, X, comp, out);
     return 1;
 }
 

@@ -55,4 +55,14 @@ int fp64_state_to_ap(const DevParams& P, const Fp64Bufs& b, int dom, const int* 
                      long long t0 = 0, long long t1 = -1);
 int fp64_prim_to_state(const DevParams& P, const Fp64Bufs& b, int dom, const double* prim, double* X, cudaStream_t st);
 
+// Deterministic binary64 sums over all valid cells of alphaRho_k (M), rhoU
+// (3) and E, each times the cell volume: out[M + 4] (device), part: scratch of
+// kConsPartials * (M + 4) doubles.
+constexpr int kConsPartials = 256;
+int fp64_conservation(const DevParams& P, const Fp64Bufs& b, const double* X, double* part, double* out, cudaStream_t st);
+// One AccessPattern component of domain dom (valid cells, i fastest) into
+// out (device).
+int fp64_state_component(const DevParams& P, const Fp64Bufs& b, int dom, const double* X, int comp, double* out,
+                         cudaStream_t st);
+
 }  // namespace tj

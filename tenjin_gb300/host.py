@@ -119,6 +119,24 @@ class TenjinGPU:
         self._check(self.L.tj_download_domain(self.h, q, _dp(out)))
         return out
 
+    def component(self, q: int, comp: int) -> np.ndarray:
+        """One AccessPattern component of domain q, shape (nz, ny, nx)."""
+        d = self.case.domains[q]
+        out = np.empty((d.n_cells[2], d.n_cells[1], d.n_cells[0]), dtype=np.float64)
+        self._check(self.L.tj_download_component(self.h, q, comp, _dp(out)))
+        return out
+
+    def density(self, q: int = 0) -> np.ndarray:
+        """rho = sum of alphaRho_k (the AccessPattern's RHO component)."""
+        return self.component(q, 3 * self.case.M)
+
+    def conservation_sums(self) -> np.ndarray:
+        """Binary64 sums over all valid cells of alphaRho_k (M), rhoU (3) and
+        E, each times the cell volume (deterministic reduction order)."""
+        out = np.empty(self.case.M + 4, dtype=np.float64)
+        self._check(self.L.tj_conservation_sums(self.h, _dp(out)))
+        return out
+
     def set_state(self, q: int, st: np.ndarray):
         st = np.ascontiguousarray(st, dtype=np.float64)
         self._check(self.L.tj_upload_domain(self.h, q, _dp(st)))

@@ -3,6 +3,7 @@ OWN hot-path sources (compiled from the reference tree through oracle/Makefile
 into oracle/_ref/) on seeded synthetic inputs.
 
 Run where the reference tree exists:  python tests/golden/make_golden.py [name ...]
+                                      python tests/golden/make_golden.py --gnuplot [name ...]
 Each fixture stores the builder call that makes its input, a SHA-256 of the
 initial primitive fields, the dt of every step and the final values of the
 carried components (AccessPattern indices listed in the file).
@@ -77,10 +78,35 @@ def prim_sha(c):
     return h.hexdigest()
 
 
+# fixtures whose final state the reference also dumps with its 1-D gnuplot
+# writer (print.cpp:33-43), stored under gnuplot/<name>/
+GNUPLOT_FIXTURES = ["sod200_boxes", "bubble4_reflect_boxes2"]
+
+
+def _make_oracle():
+    from __graft_entry__ import reference_tree
+    ref = reference_tree()
+    if not ref:
+        raise RuntimeError("the reference tree is needed: set TENJIN_REFERENCE")
+    subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "-j3", f"REF={ref}"], check=True)
+
+
+def make_gnuplot(names=None):
+    """The reference's own gnuplot dumps of the final states of
+    GNUPLOT_FIXTURES (picture 0)."""
+    for name in (names or GNUPLOT_FIXTURES):
+        d = os.path.join(HERE, "gnuplot", name)
+        os.makedirs(d, exist_ok=True)
+        for f in os.listdir(d):
+            os.remove(os.path.join(d, f))
+        refio.run_reference(build_case(name), gnuplot_dir=d)
+        print(f"{name}: gnuplot dump {sorted(os.listdir(d))}")
+
+
 def main(names=None):
     """Regenerates the named fixtures (all when none are named); the manifest
     keeps the entries of the others."""
-    subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "-j3"], check=True)
+    _make_oracle()
     manifest = {}
     mpath = os.path.join(HERE, "manifest.json")
     if names and os.path.exists(mpath):
@@ -106,4 +132,8 @@ def main(names=None):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1:])
+    if sys.argv[1:2] == ["--gnuplot"]:
+        _make_oracle()
+        make_gnuplot(sys.argv[2:])
+    else:
+        main(sys.argv[1:])

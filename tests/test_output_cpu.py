@@ -82,3 +82,47 @@ def test_picture_schedule_from_settings():
     sch = output.PictureSchedule.from_settings(cfg)
     assert sch.final_t == 0.2 and sch.pictures == 10
     assert not sch.due(0.0) and sch.due(1e-9) and not sch.due(0.02) and sch.due(0.0200001)
+
+
+GOLDEN_GNUPLOT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "gnuplot")
+
+
+def _same_files(files, ref_dir):
+    for f in files:
+        with open(f, "rb") as a, open(os.path.join(ref_dir, os.path.basename(f)), "rb") as b:
+            if a.read() != b.read():
+                return os.path.basename(f)
+    return None
+
+
+@pytest.mark.parametrize("name", ["sod200_boxes", "bubble4_reflect_boxes2", "bubble32_muscl", "copper12"])
+def test_gnuplot_dump_equals_the_reference_writer(tmp_path, name):
+    """write_gnuplot on the reference's own final state gives, byte for byte,
+    the files the reference's PrintAllVarsTo1DGnuplotFile (print.cpp:33-43,
+    compiled into the oracle harness) writes for that state."""
+    from oracle import refio
+    import fixtures as fx
+    c = fx.build_case(name)
+    if not refio.have_ref(c.dim):
+        pytest.skip("reference binaries are built only where the reference tree exists")
+    ref_dir = tmp_path / "ref"
+    ref_dir.mkdir()
+    r = refio.run_reference(c, gnuplot_dir=str(ref_dir))
+    files = output.write_gnuplot(str(tmp_path / "mine"), c, r["states"][0], 0)
+    assert sorted(os.path.basename(f) for f in files) == sorted(os.listdir(ref_dir))
+    assert _same_files(files, str(ref_dir)) is None
+
+
+@pytest.mark.parametrize("name", sorted(os.listdir(GOLDEN_GNUPLOT)) if os.path.isdir(GOLDEN_GNUPLOT) else [])
+def test_gnuplot_golden_dumps_match_the_golden_states(tmp_path, name):
+    """The committed dumps of the reference's writer agree with write_gnuplot
+    on the committed golden state (carried components; the dumped variables
+    rho, p, u, E, rhoU, alpha0 are all carried)."""
+    import fixtures as fx
+    c = fx.build_case(name)
+    gold = fx.load(name)
+    d = c.domains[0]
+    st = np.zeros((len(output.variable_names(c)), d.n_cells[2], d.n_cells[1], d.n_cells[0]))
+    st[gold["carried"]] = gold["states"][0]
+    files = output.write_gnuplot(str(tmp_path), c, st, 0)
+    assert _same_files(files, os.path.join(GOLDEN_GNUPLOT, name)) is None

@@ -103,3 +103,18 @@ def test_to_case_rejects_what_the_path_does_not_cover():
     cfg["listOfMaterials"][0]["EOS"] = "Unknown"
     with pytest.raises(settings.SettingsError):
         settings.materials(cfg)
+
+
+@pytest.mark.parametrize("name", ["sod1000_full", "sod200_boxes"])
+def test_deck_reproduces_the_fixture_input_and_the_oracle_result(name):
+    """A deck written in the reference's keys yields the fixture's initial
+    state bit for bit, and the oracle run from it the fixture's result."""
+    import fixtures as fx
+    import frontend
+    from oracle import port
+    c = frontend.deck_case(name)
+    assert fx.prim_sha(c) == fx.manifest()[name]["prim_sha256"]
+    gold = fx.load(name)
+    out = port.run_port(c)
+    assert np.array_equal(out["dts"], gold["dts"])
+    assert fx.exact_fraction(out["states"][0][gold["carried"]], gold["states"][0]) == 1.0
