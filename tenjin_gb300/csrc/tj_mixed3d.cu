@@ -21,9 +21,11 @@
 //           RK2 average (hllc.cpp:705), cleanUpAlpha (main.cpp:170), the next
 //           step's CFL minimum over all domains (timestep.cpp:36-70) and the
 //           NaN check of each domain's last box (main.cpp:183-187).
-// The tile shape (TX, TY, TZ) is a template parameter; a host-side autotuner
-// times each candidate on the actual work list once and keeps the fastest
-// (the environment variable TJ_TILE3D=AxBxC pins one candidate instead).
+// The tile shape (TX, TY, TZ) is a template parameter. The boxes fall into
+// size classes (up to 16^3 cells, up to 32^3, larger); a host-side autotuner
+// times each candidate shape on each class's tiles once and keeps the fastest
+// per class, and each class runs as its own persistent launch per stage (the
+// environment variable TJ_TILE3D=AxBxC pins one candidate for all classes).
 // Results do not depend on the tile shape (every face and cell is computed
 // by the same arithmetic whichever tile owns it).
 #include <cuda_runtime.h>
@@ -32,6 +34,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <string>
 #include <vector>
 
 #include "tj_math.cuh"
@@ -748,20 +751,48 @@ std::vector<Shape> shapes()
             make_shape<M, 4, 4, 4>()};
 }
 
+// Box-size classes of the autotuner, by valid-cell count: small boxes up to
+// 16^3 cells, medium up to 32^3, large above. Each class gets its own tile
+// shape, chosen by timing, and its own persistent launch per RK stage: the
+// boxes are independent domains, so the classes' launches need no ordering
+// among themselves beyond the stream's.
+constexpr int kClasses = 3;
+constexpr long long kClassMaxCells[kClasses - 1] = {16LL * 16 * 16, 32LL * 32 * 32};
+constexpr const char* kClassName[kClasses] = {"small", "medium", "large"};
+
+inline int box_class(const DevDomain& D)
+{
+    const long long v = (long long)D.n[0] * D.n[1] * D.n[2];
+    int c = 0;
+    while (c < kClasses - 1 && v > kClassMaxCells[c]) ++c;
+    return c;
+}
+
+// The tiles of one class under one tile shape, on the device.
+struct ClassPlan {
+    std::vector<int> doms;  // domains of the class
+    int best = -1;          // chosen shape
+    int grid = 0;
+    Work3* d_work = nullptr;
+    int nwork = 0;
+    long long cells = 0;
+    std::vector<double> tune_ms;
+};
+
 struct Mixed3D : MixedBase {
     M3P P;
     M3B b;
     int M = 0;
     float* X[2] = {nullptr, nullptr};
     Dom3* d_doms = nullptr;
-    Work3* d_work = nullptr;
+    Work3* d_work = nullptr;  // every tile of every class (the CFL pass)
     std::vector<Shape> cand;
-    int best = -1;
-    int grid = 0;
+    ClassPlan cls[kClasses];
+    bool tuned = false;
+    int sms = 0;
     long long N = 0;
     std::vector<DevDomain> hdoms;
     std::vector<std::vector<int>> hboxes;
-    std::vector<double> tune_ms;
 
     ~Mixed3D() override
     {
@@ -769,6 +800,8 @@ struct Mixed3D : MixedBase {
         if (X[1]) cudaFree(X[1]);
         if (d_doms) cudaFree(d_doms);
         if (d_work) cudaFree(d_work);
+        for (auto& c : cls)
+            if (c.d_work) cudaFree(c.d_work);
     }
 
     int alloc(const DevParams& DP, const std::vector<DevDomain>& doms, long long ntot, cudaStream_t st)
@@ -804,6 +837,9 @@ struct Mixed3D : MixedBase {
             case 3: cand = shapes<3>(); break;
             default: cand = shapes<4>(); break;
         }
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         b.X[0] = X[0];
         b.X[1] = X[1];
         b.N = N;
@@ -814,13 +850,13 @@ struct Mixed3D : MixedBase {
         return set_boxes(doms, one, st);
     }
 
-    // the work list of shape s
-    int build_work(int s, cudaStream_t st)
+    // The tiles of the given domains under shape s, largest first.
+    std::vector<Work3> tiles(const std::vector<int>& doms, int s) const
     {
         const Shape& S = cand[s];
         std::vector<Work3> work;
         std::vector<std::pair<int, int>> ax[3];
-        for (size_t q = 0; q < hdoms.size(); ++q) {
+        for (int q : doms) {
             const DevDomain& D = hdoms[q];
             split_axis(D.n[0], S.tx, ax[0]);
             split_axis(D.n[1], S.ty, ax[1]);
@@ -829,7 +865,7 @@ struct Mixed3D : MixedBase {
                 for (auto& y : ax[1])
                     for (auto& x : ax[0]) {
                         Work3 w;
-                        w.dom = (int)q;
+                        w.dom = q;
                         w.i0 = (short)x.first;
                         w.j0 = (short)y.first;
                         w.k0 = (short)z.first;
@@ -843,19 +879,54 @@ struct Mixed3D : MixedBase {
         // largest tiles first: the persistent CTAs balance the tail
         std::stable_sort(work.begin(), work.end(),
                          [](const Work3& a, const Work3& c) { return a.ex * a.ey * a.ez > c.ex * c.ey * c.ez; });
-        if (d_work) cudaFree(d_work);
-        d_work = nullptr;
-        if (cudaMalloc(&d_work, sizeof(Work3) * std::max<size_t>(work.size(), 1)) != cudaSuccess) return TJ_ERR_CUDA;
-        cudaMemcpyAsync(d_work, work.data(), sizeof(Work3) * work.size(), cudaMemcpyHostToDevice, st);
+        return work;
+    }
+
+    static int upload(Work3*& dst, const std::vector<Work3>& w, cudaStream_t st)
+    {
+        if (dst) cudaFree(dst);
+        dst = nullptr;
+        if (cudaMalloc(&dst, sizeof(Work3) * std::max<size_t>(w.size(), 1)) != cudaSuccess) return TJ_ERR_CUDA;
+        if (!w.empty()) cudaMemcpyAsync(dst, w.data(), sizeof(Work3) * w.size(), cudaMemcpyHostToDevice, st);
         cudaStreamSynchronize(st);
-        b.work = d_work;
-        b.nwork = (int)work.size();
-        int dev = 0, sms = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        const int occ = std::max(1, S.occupancy(S.smem));
-        grid = std::max(1, std::min(b.nwork, sms * occ));
         return TJ_OK;
+    }
+
+    // Class c's work list under shape s, on the device, and its grid.
+    int plan_class(int c, int s, cudaStream_t st)
+    {
+        ClassPlan& C = cls[c];
+        const std::vector<Work3> w = tiles(C.doms, s);
+        if (int e = upload(C.d_work, w, st)) return e;
+        C.nwork = (int)w.size();
+        C.best = s;
+        const Shape& S = cand[s];
+        const int occ = std::max(1, S.occupancy(S.smem));
+        C.grid = std::max(1, std::min(C.nwork, sms * occ));
+        return TJ_OK;
+    }
+
+    // The CFL pass's work list: every tile of every class under its shape.
+    int plan_all(cudaStream_t st)
+    {
+        std::vector<Work3> all;
+        for (int c = 0; c < kClasses; ++c) {
+            if (cls[c].doms.empty()) continue;
+            const std::vector<Work3> w = tiles(cls[c].doms, std::max(0, cls[c].best));
+            all.insert(all.end(), w.begin(), w.end());
+        }
+        if (int e = upload(d_work, all, st)) return e;
+        b.work = d_work;
+        b.nwork = (int)all.size();
+        return TJ_OK;
+    }
+
+    M3B class_bufs(int c) const
+    {
+        M3B bc = b;
+        bc.work = cls[c].d_work;
+        bc.nwork = cls[c].nwork;
+        return bc;
     }
 
     int set_boxes(const std::vector<DevDomain>& doms, const std::vector<std::vector<int>>& boxes,
@@ -864,6 +935,10 @@ struct Mixed3D : MixedBase {
         hdoms = doms;
         hboxes = boxes;
         std::vector<Dom3> d3(doms.size());
+        for (auto& c : cls) {
+            c.doms.clear();
+            c.cells = 0;
+        }
         for (size_t q = 0; q < doms.size(); ++q) {
             const DevDomain& D = doms[q];
             for (int k = 0; k < 3; ++k) {
@@ -876,57 +951,71 @@ struct Mixed3D : MixedBase {
             const std::vector<int>& bl = boxes[q];
             const int* L = &bl[bl.size() - 6];
             for (int k = 0; k < 6; ++k) d3[q].last[k] = L[k];
+            ClassPlan& C = cls[box_class(D)];
+            C.doms.push_back((int)q);
+            C.cells += (long long)D.n[0] * D.n[1] * D.n[2];
         }
         if (d_doms) cudaFree(d_doms);
         d_doms = nullptr;
         if (cudaMalloc(&d_doms, sizeof(Dom3) * d3.size()) != cudaSuccess) return TJ_ERR_CUDA;
         cudaMemcpyAsync(d_doms, d3.data(), sizeof(Dom3) * d3.size(), cudaMemcpyHostToDevice, st);
         b.doms = d_doms;
-        best = -1;  // re-tune on the next upload
-        return build_work(0, st);
+        tuned = false;  // re-tune on the next upload
+        for (int c = 0; c < kClasses; ++c)
+            if (!cls[c].doms.empty())
+                if (int e = plan_class(c, 0, st)) return e;
+        return plan_all(st);
     }
 
-    // Times one stage launch per candidate shape on the current state and
-    // keeps the fastest (the trial results are discarded: the stage-1 output
-    // buffer is scratch until the next step).
+    // For each box-size class, times one stage launch per candidate shape
+    // over that class's tiles on the current state and keeps the fastest
+    // (the trial results are discarded: the stage-1 output buffer is scratch
+    // until the next step). TJ_TILE3D=AxBxC pins one candidate for every
+    // class instead.
     void autotune(cudaStream_t st)
     {
-        // TJ_TILE3D=AxBxC pins the tile shape (one of the candidates)
+        int pinned = -1;
         if (const char* env = std::getenv("TJ_TILE3D")) {
             int a = 0, c = 0, d = 0;
             if (std::sscanf(env, "%dx%dx%d", &a, &c, &d) == 3)
                 for (size_t s = 0; s < cand.size(); ++s)
-                    if (cand[s].tx == a && cand[s].ty == c && cand[s].tz == d) {
-                        best = (int)s;
-                        build_work(best, st);
-                        return;
-                    }
+                    if (cand[s].tx == a && cand[s].ty == c && cand[s].tz == d) pinned = (int)s;
         }
         cudaEvent_t e0, e1;
         cudaEventCreate(&e0);
         cudaEventCreate(&e1);
-        tune_ms.assign(cand.size(), 0.0);
-        float bestms = 3e38f;
-        int bi = 0;
-        for (size_t s = 0; s < cand.size(); ++s) {
-            if (build_work((int)s, st) != TJ_OK) continue;
-            cand[s].stage(P, b, 0, 1, grid, cand[s].smem, st);  // warm-up
-            cudaEventRecord(e0, st);
-            for (int r = 0; r < 3; ++r) cand[s].stage(P, b, 0, 1, grid, cand[s].smem, st);
-            cudaEventRecord(e1, st);
-            cudaEventSynchronize(e1);
-            float ms = 0.0f;
-            cudaEventElapsedTime(&ms, e0, e1);
-            tune_ms[s] = ms / 3.0;
-            if (ms < bestms) {
-                bestms = ms;
-                bi = (int)s;
+        for (int c = 0; c < kClasses; ++c) {
+            ClassPlan& C = cls[c];
+            if (C.doms.empty()) continue;
+            if (pinned >= 0) {
+                plan_class(c, pinned, st);
+                continue;
             }
+            C.tune_ms.assign(cand.size(), 0.0);
+            float bestms = 3e38f;
+            int bi = 0;
+            for (size_t s = 0; s < cand.size(); ++s) {
+                if (plan_class(c, (int)s, st) != TJ_OK) continue;
+                const M3B bc = class_bufs(c);
+                cand[s].stage(P, bc, 0, 1, C.grid, cand[s].smem, st);  // warm-up
+                cudaEventRecord(e0, st);
+                for (int r = 0; r < 3; ++r) cand[s].stage(P, bc, 0, 1, C.grid, cand[s].smem, st);
+                cudaEventRecord(e1, st);
+                cudaEventSynchronize(e1);
+                float ms = 0.0f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                C.tune_ms[s] = ms / 3.0;
+                if (ms < bestms) {
+                    bestms = ms;
+                    bi = (int)s;
+                }
+            }
+            plan_class(c, bi, st);
         }
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
-        best = bi;
-        build_work(best, st);
+        plan_all(st);
+        tuned = true;
         cudaGetLastError();
     }
 
@@ -939,7 +1028,7 @@ struct Mixed3D : MixedBase {
             case 3: k_from_fp64_3d<3><<<nblk3(N), 256, 0, st>>>(DP, b, fb.A); break;
             default: k_from_fp64_3d<4><<<nblk3(N), 256, 0, st>>>(DP, b, fb.A); break;
         }
-        if (best < 0) autotune(st);
+        if (!tuned) autotune(st);
         return 1 + cfl(fb, st);
     }
 
@@ -972,22 +1061,34 @@ struct Mixed3D : MixedBase {
     {
         b.scal = fb.scal;
         int n = fp64_dt_finalize(DP, fb, 1, st);
-        const Shape& S = cand[best < 0 ? 0 : best];
-        for (int stage = 0; stage < 2; ++stage) {
-            if (pr) pr->begin("tj_stage3d_mixed", st);
-            S.stage(P, b, stage, 0, grid, S.smem, st);
-            if (pr) pr->end("tj_stage3d_mixed", st);
-            n += 1;
-        }
+        for (int stage = 0; stage < 2; ++stage)
+            for (int c = 0; c < kClasses; ++c) {
+                const ClassPlan& C = cls[c];
+                if (C.doms.empty()) continue;
+                const Shape& S = cand[C.best < 0 ? 0 : C.best];
+                if (pr) pr->begin("tj_stage3d_mixed", st);
+                S.stage(P, class_bufs(c), stage, 0, C.grid, S.smem, st);
+                if (pr) pr->end("tj_stage3d_mixed", st);
+                n += 1;
+            }
         n += fp64_step_end(fb, st);
         return n;
     }
 
     void describe(char* buf, size_t len) const override
     {
-        const Shape& S = cand[best < 0 ? 0 : best];
-        std::snprintf(buf, len, "tile %dx%dx%d, %d tiles, grid %d, smem %zu B", S.tx, S.ty, S.tz, b.nwork, grid,
-                      S.smem);
+        std::string out;
+        for (int c = 0; c < kClasses; ++c) {
+            const ClassPlan& C = cls[c];
+            if (C.doms.empty()) continue;
+            const Shape& S = cand[C.best < 0 ? 0 : C.best];
+            char line[192];
+            std::snprintf(line, sizeof line, "%s%s boxes (%zu, %lld cells): tile %dx%dx%d, %d tiles, grid %d, smem %zu B",
+                          out.empty() ? "" : "; ", kClassName[c], C.doms.size(), C.cells, S.tx, S.ty, S.tz, C.nwork,
+                          C.grid, S.smem);
+            out += line;
+        }
+        std::snprintf(buf, len, "%s", out.c_str());
     }
 };
 

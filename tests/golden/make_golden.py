@@ -33,9 +33,11 @@ FIXTURES = {
     "bubble40_reflect": ("shock_bubble_2d", {"n": 40, "max_grid_size": 16, "max_steps": 40, "radius": 0.3},
                          {"lo_bc": [1, 1, 0], "hi_bc": [1, 0, 0]}),
     "bubble32_muscl": ("shock_bubble_2d", {"n": 32, "max_grid_size": 32, "max_steps": 30, "thinc": 0}),
-    "uneven3d_4dom": ("uneven_boxes_3d", {"nbox": 4, "lo": 6, "hi": 10, "max_steps": 8}),
-    "fluid3d_boxes": ("fluid_boxes_3d", {"n": 12, "max_grid_size": 5, "max_steps": 5}),
-    "copper12": ("copper_plate_3d", {"n": 12, "max_grid_size": 6, "max_steps": 8}),
+    # the 3-D fixtures were made at CFL 0.4 (short runs, before the 3-D
+    # workloads moved to cases.CFL_3D)
+    "uneven3d_4dom": ("uneven_boxes_3d", {"nbox": 4, "lo": 6, "hi": 10, "max_steps": 8, "cfl": 0.4}),
+    "fluid3d_boxes": ("fluid_boxes_3d", {"n": 12, "max_grid_size": 5, "max_steps": 5, "cfl": 0.4}),
+    "copper12": ("copper_plate_3d", {"n": 12, "max_grid_size": 6, "max_steps": 8, "cfl": 0.4}),
     "wilkins2d_plastic": ("solid_mixture_2d", {"eos": cases.EOS_WILKINS, "n": 20, "max_steps": 10}),
     "romenskii2d_plastic": ("solid_mixture_2d", {"eos": cases.EOS_ROMENSKII, "n": 20, "max_steps": 10}),
     "hugoniot2d_plastic": ("solid_mixture_2d", {"eos": cases.EOS_HUGONIOT, "n": 16, "max_steps": 10}),

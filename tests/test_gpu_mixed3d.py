@@ -79,3 +79,38 @@ def test_mixed3d_result_independent_of_tile_shape(tmp_path):
         outs.append(np.load(f))
     for o in outs[1:]:
         assert np.array_equal(o, outs[0])
+
+
+_CLASS_SCRIPT = r"""
+import ctypes, sys, numpy as np
+sys.path.insert(0, sys.argv[1])
+from tenjin_gb300 import cases
+from tenjin_gb300.host import MIXED, TenjinGPU
+c = cases.uneven_boxes_3d(nbox=16, seed=7, lo=6, hi=44, max_steps=5)
+g = TenjinGPU(c, MIXED)
+g.run(5, 1e300)
+buf = ctypes.create_string_buffer(1024)
+g.L.tj_kernel_config(g.h, buf, 1024)
+print(buf.value.decode())
+np.save(sys.argv[2], np.concatenate([g.state(q).ravel() for q in range(len(c.domains))]))
+"""
+
+
+def test_mixed3d_size_classes_tuned_apart_give_the_pinned_result(tmp_path):
+    """Boxes of all three size classes: the autotuner plans each class on its
+    own (one launch per class and stage) and reports a tile per class; the
+    state equals the one with a single pinned tile shape, bit for bit."""
+    outs, cfg = [], []
+    for shape in (None, "8x8x4"):
+        f = tmp_path / f"s{shape}.npy"
+        env = dict(os.environ)
+        env.pop("TJ_TILE3D", None)
+        if shape:
+            env["TJ_TILE3D"] = shape
+        r = subprocess.run([sys.executable, "-c", _CLASS_SCRIPT, ROOT, str(f)], check=True, env=env, timeout=600,
+                           capture_output=True, text=True)
+        cfg.append(r.stdout.strip().splitlines()[-1])
+        outs.append(np.load(f))
+    assert all(k in cfg[0] for k in ("small boxes", "medium boxes", "large boxes")), cfg[0]
+    assert cfg[1].count("tile 8x8x4") == 3, cfg[1]
+    assert np.array_equal(outs[0], outs[1])
