@@ -128,6 +128,13 @@ def l2_flush_bytes():
     return 256 << 20  # larger than the 129 MB L2
 
 
+def bench_config(args, ws):
+    """The `config` object of the JSON line, the same for both arms."""
+    return {"workload": WORKLOAD, "cells": N_CELLS * N_CELLS, "precision": args.precision,
+            "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
+            "l2": "state working set larger than L2 (three state buffers of >= 48 MB plus scratch per step)"}
+
+
 def run_gpu_arm(args):
     import torch
 
@@ -273,9 +280,7 @@ def run_gpu_arm(args):
         "vs_baseline": None, "dtype": {MIXED: "f32 (compensated energy and pressure closure)", FUSED64: "f64 (fused kernels)",
                                         FP64: "f64"}[precision],
         "data": "synthetic (seeded shock-bubble initial condition)",
-        "config": {"workload": WORKLOAD, "cells": ncell, "precision": args.precision,
-                   "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
-                   "l2": "state working set larger than L2 (three state buffers of >= 48 MB plus scratch per step)"},
+        "config": bench_config(args, ws),
         "gpu_launches": launches, "steps_done": done, "e2e": e2e, "roofline": roofline, "clocks": clocks,
         "accuracy": accuracy, "adjoint": adjoint, "other_configs": configs,
     }
@@ -340,7 +345,8 @@ def other_configs():
                   "ms_per_step": ms32 / max(d32, 1), "kernel_config": buf.value.decode()},
         "fp64": {"value": c.total_cells * d64 / (ms64 / 1e3), "unit": "cell-updates/s", "steps": d64,
                  "ms_per_step": ms64 / max(d64, 1)},
-        "l1_rel_density_err_after_5_steps": e, "sampled_boxes": len(sample)}
+        "l1_rel_density_err_after_5_steps": e, "sampled_boxes": len(sample),
+        "whole_run": horizon("boxes", cases.uneven_boxes_3d(nbox=512), 100)}
     c = cases.copper_plate_3d(n=256)
     g = TenjinGPU(c, FP64)
     g.run(1, 1e300)
@@ -361,51 +367,58 @@ def other_configs():
                  "ms_per_step": ms / max(d, 1)},
         "mixed": {"value": c.total_cells * d32b / (ms32b / 1e3), "unit": "cell-updates/s", "steps": d32b,
                   "ms_per_step": ms32b / max(d32b, 1), "kernel_config": buf.value.decode()},
-        "l1_rel_density_err_after_3_steps": float(abs(r32 - r64).sum() / abs(r64).sum())}
+        "l1_rel_density_err_after_3_steps": float(abs(r32 - r64).sum() / abs(r64).sum()),
+        "whole_run": horizon("copper", cases.copper_plate_3d(n=64), 500)}
     return out
 
 
+def horizon(name, case, steps):
+    """Binary32 against the reference-ordered binary64 path over a whole run
+    (relative L1 and Linf density difference every steps/10 steps), at a
+    reduced size so that the binary64 run takes seconds."""
+    from tenjin_gb300 import accuracy
+    from tenjin_gb300.host import FP64, MIXED
+
+    curves = accuracy.density_curves(case, {"fp64": (case, FP64), "mixed": (case, MIXED)}, [("mixed", "fp64")],
+                                     steps, max(1, steps // 10))
+    p = curves["pairs"]["mixed_vs_fp64"]
+    return {"cells": case.total_cells, "steps": steps, "cfl": case.cfl, "curve_steps": curves["steps"],
+            "l1_rel": p["l1"], "linf_rel": p["linf"], "l1_max": max(p["l1"])}
+
+
 def accuracy_runs(case, steps):
-    """The workload for `steps` steps from its initial state in binary32
-    (TJ_PRECISION_MIXED), in binary64 through the same fused kernels
-    (TJ_PRECISION_FUSED64) and through the reference-ordered FP64 kernels
-    (TJ_PRECISION_FP64): the relative L1 and Linf errors of the density field
-    (sum of alphaRho) between each pair, and each run's throughput."""
-    import torch
+    """The workload for `steps` steps from its initial state through the
+    binary32 kernels (TJ_PRECISION_MIXED), the same fused kernels in binary64
+    (TJ_PRECISION_FUSED64), the reference-ordered binary64 kernels
+    (TJ_PRECISION_FP64), and the binary64 kernels from the initial state
+    perturbed by 1e-14 and from it rounded to binary32 once: relative L1 and
+    Linf density differences every 100 steps (tenjin_gb300.accuracy), the
+    criterion along the run, each run's throughput, and the binary64 global
+    conservation sums (tj_conservation_sums) at the start and the end."""
+    from tenjin_gb300 import accuracy
 
-    from tenjin_gb300.host import FP64, FUSED64, MIXED, TenjinGPU
-
+    runs, pairs = accuracy.plan("bubble", case)
+    curves = accuracy.density_curves(case, runs, pairs, steps, 100, sums=True)
+    summ = accuracy.summarise(curves)
+    sums = {k: curves["sums"][k] for k in ("fp64", "fused64", "mixed")}
     M = case.M
-    dens, speed, tend = {}, {}, {}
-    for name, prec in (("mixed", MIXED), ("fused64", FUSED64), ("fp64", FP64)):
-        g = TenjinGPU(case, prec)
-        sp = ctypes.c_void_p()
-        g.L.tj_get_stream(g.h, ctypes.byref(sp))
-        st = torch.cuda.ExternalStream(sp.value)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        torch.cuda.synchronize()
-        with torch.cuda.stream(st):
-            e0.record(st)
-        done, t = g.run(steps, 1e300)
-        with torch.cuda.stream(st):
-            e1.record(st)
-        torch.cuda.synchronize()
-        ms = e0.elapsed_time(e1)
-        dens[name] = g.state(0)[M:2 * M].sum(axis=0)
-        speed[name] = {"value": case.total_cells * done / (ms / 1e3), "unit": "cell-updates/s",
-                       "ms_per_step": ms / max(done, 1)}
-        tend[name] = t
-        g.close()
-
-    def err(a, b):
-        e = abs(dens[a] - dens[b])
-        return {"l1_rel": float(e.sum() / abs(dens[b]).sum()), "linf_rel": float(e.max() / abs(dens[b]).max())}
-
-    return {"steps": steps, "field": "density (sum of alphaRho)",
-            "mixed_vs_fused64": err("mixed", "fused64"), "mixed_vs_fp64": err("mixed", "fp64"),
-            "fused64_vs_fp64": err("fused64", "fp64"), "t_end": tend, "throughput": speed,
-            "note": "fused64 and fp64 differ only by rounding; their difference is the FP64 round-off floor "
-                    "of this chaotic interface flow"}
+    rel = lambda a, b: abs(a - b) / abs(b)
+    cons = {"layout": f"[alphaRho_0..{M - 1}, rhoU_x, rhoU_y, rhoU_z, E] x cell volume, binary64, fixed order",
+            "runs": sums,
+            "mixed_vs_fp64_end": {"mass": [rel(sums["mixed"]["end"][m], sums["fp64"]["end"][m]) for m in range(M)],
+                                  "energy": rel(sums["mixed"]["end"][M + 3], sums["fp64"]["end"][M + 3])},
+            "note": "the boundaries are transmissive (the shock enters at x = 0), so the sums change over the run "
+                    "in every precision; their agreement between precisions is the check"}
+    sec = curves["seconds"]
+    speed = {k: {"value": case.total_cells * steps / sec[k], "unit": "cell-updates/s",
+                 "ms_per_step": 1e3 * sec[k] / steps, "timing": "host wall time of the run blocks"}
+             for k in ("mixed", "fused64", "fp64")}
+    return {"steps": steps, "field": "density (sum of alphaRho)", "sampled_every": 100,
+            "pairs": summ, "curve_steps": curves["steps"],
+            "curves_l1": {k: v["l1"] for k, v in curves["pairs"].items()},
+            "t_end": {k: v[-1] for k, v in curves["t"].items()}, "throughput": speed, "conservation": cons,
+            "note": "fused64 vs fp64 and fp64_pert vs fp64 are the binary64 floor of this chaotic interface "
+                    "flow; fp64_f32 vs fp64 is what one rounding of the state to binary32 grows to"}
 
 
 def cpu_baseline(target_seconds=15.0):
@@ -464,9 +477,10 @@ def run_reference_arm(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded shock-bubble initial condition)",
-        "config": {"workload": WORKLOAD, "sample": f"{side}x{side} cells (max_grid_size {mgs})"},
+        "config": bench_config(args, ws),
         "cpu_baseline": {"value": value, "unit": "cell-updates/s", "cores": nthr, "kind": "port",
-                         "sample": f"{args.steps} steps of a {side}x{side} sample of the workload"},
+                         "sample": f"{args.steps} steps of a {side}x{side} sample of the workload "
+                                   f"(max_grid_size {mgs}), FP64"},
         "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)

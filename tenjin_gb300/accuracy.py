@@ -17,11 +17,15 @@ Runs:
   fused64    TJ_PRECISION_FUSED64, the fused 2-D kernels in binary64 (2-D only)
   fp64_pert  fp64 from an initial pressure multiplied by 1 + 1e-14 * xi, xi
              seeded uniform in [-1, 1]: a few units in the last place
+  fp64_f32   fp64 from the initial primitive fields rounded to binary32 once:
+             the state a binary32 run starts from, advanced in binary64
 
 fp64_pert vs fp64 measures how fast the flow itself amplifies a last-bit
 difference, and fused64 vs fp64 what a different but equally exact binary64
 evaluation order gives: together they are the binary64 floor of any
-comparison against the reference on this flow. The workloads are the
+comparison against the reference on this flow. fp64_f32 vs fp64 is what one
+rounding of the state to binary32 grows to: a floor for any method that
+stores the state in binary32. The workloads are the
 benchmark's: the 2-D shock-bubble (1024^2, THINC, max_grid_size 128), the
 copper plate (n^3, radial return) and the batch of uneven 3-D boxes.
 """
@@ -51,6 +55,14 @@ def perturbed(case, eps: float = PERTURBATION, seed: int = 1234):
     return c
 
 
+def rounded_to_binary32(case):
+    """A copy of `case` whose initial primitive fields are rounded to binary32."""
+    c = copy.deepcopy(case)
+    for d in c.domains:
+        d.prim = d.prim.astype(np.float32).astype(np.float64)
+    return c
+
+
 def _density(g, ndom):
     return np.concatenate([g.density(q).ravel() for q in range(ndom)])
 
@@ -60,14 +72,18 @@ def _diff(a, b):
     return float(e.sum() / np.abs(b).sum()), float(e.max() / np.abs(b).max())
 
 
-def density_curves(case, runs, pairs, steps: int, every: int):
+def density_curves(case, runs, pairs, steps: int, every: int, sums: bool = False):
     """Run each of `runs` ({name: (case, precision)}) for `steps` steps in
     blocks of `every`; after each block record the density differences of
-    each pair (a, b) in `pairs`. Returns a dict of lists per pair."""
+    each pair (a, b) in `pairs`. Returns a dict of lists per pair; with
+    `sums`, also each run's binary64 conservation sums at the start and the
+    end (tj_conservation_sums)."""
     ctx = {k: TenjinGPU(c, p) for k, (c, p) in runs.items()}
     ndom = len(case.domains)
     out = {"steps": [], "t": {k: [] for k in runs}, "pairs": {f"{a}_vs_{b}": {"l1": [], "linf": []} for a, b in pairs},
            "seconds": {k: 0.0 for k in runs}}
+    if sums:
+        out["sums"] = {k: {"start": g.conservation_sums().tolist()} for k, g in ctx.items()}
     done = 0
     try:
         while done < steps:
@@ -86,13 +102,16 @@ def density_curves(case, runs, pairs, steps: int, every: int):
                 l1, linf = _diff(dens[a], dens[b])
                 out["pairs"][f"{a}_vs_{b}"]["l1"].append(l1)
                 out["pairs"][f"{a}_vs_{b}"]["linf"].append(linf)
+        if sums:
+            for k, g in ctx.items():
+                out["sums"][k]["end"] = g.conservation_sums().tolist()
     finally:
         for g in ctx.values():
             g.close()
     return out
 
 
-def floor_gate(curves, run: str = "mixed_vs_fp64", floors=("fused64_vs_fp64", "fp64_pert_vs_fp64"),
+def floor_gate(curves, run: str = "mixed_vs_fp64", floors=("fused64_vs_fp64", "fp64_pert_vs_fp64", "fp64_f32_vs_fp64"),
                tol: float = 1e-4, factor: float = 2.0):
     """The mixed-precision criterion along the curve: at every sample the L1
     difference of `run` is at most max(tol, factor x the binary64 floor),
@@ -120,8 +139,9 @@ def workload(name: str, n: int = 0, nbox: int = 0):
 
 
 def plan(name: str, case):
-    runs = {"fp64": (case, FP64), "mixed": (case, MIXED), "fp64_pert": (perturbed(case), FP64)}
-    pairs = [("mixed", "fp64"), ("fp64_pert", "fp64")]
+    runs = {"fp64": (case, FP64), "mixed": (case, MIXED), "fp64_pert": (perturbed(case), FP64),
+            "fp64_f32": (rounded_to_binary32(case), FP64)}
+    pairs = [("mixed", "fp64"), ("fp64_pert", "fp64"), ("fp64_f32", "fp64")]
     if name == "bubble":
         runs["fused64"] = (case, FUSED64)
         pairs += [("fused64", "fp64"), ("mixed", "fused64")]

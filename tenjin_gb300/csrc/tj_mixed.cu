@@ -230,6 +230,119 @@ __device__ __forceinline__ void p2c_f(const MixP<R>& P, const R* rk, FaceS<R, M>
     s.c = RT<R>::sqrt_(sa / xt);
 }
 
+// ---- paired binary32 arithmetic: the two reconstructed states of a cell ----
+// A cell's left and right face states (UL, UR) go through the same sequence
+// of operations (MUSCL, cleanUpAlpha, primitiveToConservative, getSoundSpeed),
+// so the binary32 instance carries them as pairs (x = UL, y = UR) and uses
+// Blackwell's paired FFMA2 / FADD2 / FMUL2 instructions: one instruction for
+// both states. Every component is rounded as its scalar counterpart would be.
+__device__ __forceinline__ float2 f2(float x, float y) { return make_float2(x, y); }
+__device__ __forceinline__ float2 f2s(float v) { return make_float2(v, v); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+// fast reciprocal of each component (the -use_fast_math division's)
+__device__ __forceinline__ float2 rcp2(float2 a) { return f2(__fdividef(1.0f, a.x), __fdividef(1.0f, a.y)); }
+
+// MUSCL of one primitive: (UL, UR) = u0 -/+ g/2 (muscl_f).
+__device__ __forceinline__ float2 muscl_pair(float um, float u0, float up)
+{
+    const float a = u0 - um, b = up - u0;
+    float g = 0.0f;
+    if (a * b > 0.0f) g = (fabsf(a) < fabsf(b)) ? a : b;
+    return fma2(f2(-0.5f, 0.5f), f2s(g), f2s(u0));
+}
+
+// cleanUpAlpha of both states (cleanup_f, componentwise).
+template <int M>
+__device__ __forceinline__ void cleanup_pair(float2* a)
+{
+    float2 tot = f2s(0.0f);
+    int nanx = 0, nany = 0;
+#pragma unroll
+    for (int m = 0; m < M; ++m) {
+        float vx = a[m].x, vy = a[m].y;
+        if (isnan(vx)) { vx = 0.0f; if (nanx == 0) nanx = m; }
+        else if (vx < 0.0f) vx = 1e-6f;
+        else if (vx > 1.0f) vx = 1.0f;
+        if (isnan(vy)) { vy = 0.0f; if (nany == 0) nany = m; }
+        else if (vy < 0.0f) vy = 1e-6f;
+        else if (vy > 1.0f) vy = 1.0f;
+        a[m] = f2(vx, vy);
+        tot = add2(tot, a[m]);
+    }
+    if (nanx > 0) { a[nanx].x = 1.0f - tot.x; tot.x += a[nanx].x; }
+    if (nany > 0) { a[nany].y = 1.0f - tot.y; tot.y += a[nany].y; }
+    const float2 it = rcp2(tot);
+#pragma unroll
+    for (int m = 0; m < M; ++m) a[m] = mul2(a[m], it);
+}
+
+// primitiveToConservative + getSoundSpeed (p2c_f) of both states, written
+// into L (x) and R (y).
+template <int M>
+__device__ __forceinline__ void p2c_pair(const MixP<float>& P, const float2* a, const float2* rk, const float2* u,
+                                         float2 p, FaceS<float, M>& L, FaceS<float, M>& R)
+{
+    float2 ar[M], rho = f2s(0.0f);
+#pragma unroll
+    for (int m = 0; m < M; ++m) {
+        ar[m] = mul2(a[m], rk[m]);
+        rho = add2(rho, ar[m]);
+    }
+    const float2 hr = mul2(f2s(0.5f), rho);
+    float2 ru[2], ke = f2s(0.0f);
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+        ru[r] = mul2(u[r], rho);
+        ke = fma2(mul2(hr, u[r]), u[r], ke);
+    }
+    float2 G = f2s(0.0f), ec = f2s(0.0f), pc = f2s(0.0f);
+#pragma unroll
+    for (int m = 0; m < M; ++m) {
+        G = fma2(a[m], f2s(P.ig[m]), G);
+        ec = fma2(f2s(P.eref[m]), ar[m], ec);
+        pc = fma2(mul2(f2s(P.pref[m]), a[m]), f2s(P.ig[m]), pc);
+    }
+    const float2 E = add2(fma2(p, G, add2(ec, mul2(f2s(-1.0f), pc))), ke);
+    const float2 irho = rcp2(rho);
+    float2 xt = f2s(0.0f);
+    float sax = 0.0f, say = 0.0f;
+#pragma unroll
+    for (int m = 0; m < M; ++m) {
+        const float2 irk = rcp2(rk[m]);
+        const float2 c2 = mul2(fma2(p, f2s(P.g[m] + 1.0f), f2s(-P.pref[m])), irk);
+        const float2 v = mul2(mul2(f2s(P.ig[m]), c2), mul2(ar[m], irho));
+        sax += (0.0f < v.x) ? v.x : 0.0f;
+        say += (0.0f < v.y) ? v.y : 0.0f;
+        xt = fma2(f2s(P.ig[m]), a[m], xt);
+    }
+    if (sax <= 0.0f) sax = 1e-6f;
+    if (say <= 0.0f) say = 1e-6f;
+#pragma unroll
+    for (int m = 0; m < M; ++m) {
+        L.a[m] = a[m].x;
+        R.a[m] = a[m].y;
+        L.ar[m] = ar[m].x;
+        R.ar[m] = ar[m].y;
+    }
+    L.rho = rho.x;
+    R.rho = rho.y;
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+        L.ru[r] = ru[r].x;
+        R.ru[r] = ru[r].y;
+        L.u[r] = u[r].x;
+        R.u[r] = u[r].y;
+    }
+    L.E = E.x;
+    R.E = E.y;
+    L.p = p.x;
+    R.p = p.y;
+    L.c = sqrtf(sax / xt.x);
+    R.c = sqrtf(say / xt.y);
+}
+
 template <typename R, int M>
 struct Flux {
     R f[2 * M + 4];  // alpha[M], alphaRho[M], rhoU (2), E; f[2M+3] = S*
@@ -410,7 +523,13 @@ __device__ void sweep_line(const MixP<R>& P, const MixB<R>& b, R* sm, int x0, in
     for (int q = 0; q < NP; ++q) {
         const R* Q = sU + q * MS * MP;
         const R um = Q[(ty - oy) * MP + tx - ox], u0 = Q[ty * MP + tx], up = Q[(ty + oy) * MP + tx + ox];
-        muscl_f<R>(um, u0, up, ul[q], ur[q]);
+        if constexpr (sizeof(R) == 4) {
+            const float2 lr = muscl_pair(um, u0, up);
+            ul[q] = lr.x;
+            ur[q] = lr.y;
+        } else {
+            muscl_f<R>(um, u0, up, ul[q], ur[q]);
+        }
     }
     // ---- BVD-THINC (thinc.cpp:67-208) ----
     Cand<R> cd;
@@ -492,27 +611,40 @@ __device__ void sweep_line(const MixP<R>& P, const MixB<R>& b, R* sm, int x0, in
     }
     // ---- cleanUpAlpha, primitiveToConservative, getSoundSpeed ----
     FaceS<R, M> SLs, SRs;
-    R rkl[M], rkr[M];
+    if constexpr (sizeof(R) == 4) {
+        float2 a2[M], rk2[M], u2[2];
 #pragma unroll
-    for (int m = 0; m < M; ++m) {
-        SLs.a[m] = ul[m];
-        SRs.a[m] = ur[m];
-        rkl[m] = ul[M + m];
-        rkr[m] = ur[M + m];
-    }
-    if (THINC) {
-        cleanup_f<R, M>(SLs.a);
-        cleanup_f<R, M>(SRs.a);
-    }
+        for (int m = 0; m < M; ++m) {
+            a2[m] = f2(ul[m], ur[m]);
+            rk2[m] = f2(ul[M + m], ur[M + m]);
+        }
+        if (THINC) cleanup_pair<M>(a2);
 #pragma unroll
-    for (int r = 0; r < 2; ++r) {
-        SLs.u[r] = ul[2 * M + r];
-        SRs.u[r] = ur[2 * M + r];
+        for (int r = 0; r < 2; ++r) u2[r] = f2(ul[2 * M + r], ur[2 * M + r]);
+        p2c_pair<M>(P, a2, rk2, u2, f2(ul[2 * M + 2], ur[2 * M + 2]), SLs, SRs);
+    } else {
+        R rkl[M], rkr[M];
+#pragma unroll
+        for (int m = 0; m < M; ++m) {
+            SLs.a[m] = ul[m];
+            SRs.a[m] = ur[m];
+            rkl[m] = ul[M + m];
+            rkr[m] = ur[M + m];
+        }
+        if (THINC) {
+            cleanup_f<R, M>(SLs.a);
+            cleanup_f<R, M>(SRs.a);
+        }
+#pragma unroll
+        for (int r = 0; r < 2; ++r) {
+            SLs.u[r] = ul[2 * M + r];
+            SRs.u[r] = ur[2 * M + r];
+        }
+        SLs.p = ul[2 * M + 2];
+        SRs.p = ur[2 * M + 2];
+        p2c_f<R, M>(P, rkl, SLs);
+        p2c_f<R, M>(P, rkr, SRs);
     }
-    SLs.p = ul[2 * M + 2];
-    SRs.p = ur[2 * M + 2];
-    p2c_f<R, M>(P, rkl, SLs);
-    p2c_f<R, M>(P, rkr, SRs);
 
     // ---- ghost lanes take the boundary image of a valid lane's state ----
     if (p0 < 0 || p0 + 31 >= n) {  // only lines that reach the domain boundary
