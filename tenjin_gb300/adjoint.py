@@ -230,7 +230,13 @@ if __name__ == "__main__":
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--stride", type=int, default=20)
     ap.add_argument("--dirs", type=int, default=64)
+    ap.add_argument("--step-rho", type=float, default=1e-8, help="relative step along the partial densities")
+    ap.add_argument("--step-eos", type=float, default=1e-6, help="relative step along (gamma, p_ref)")
+    ap.add_argument("--background", type=float, default=1e-3,
+                    help="relative amplitude of the smooth background of the base state (0: the configuration as "
+                         "stated, with exactly uniform regions)")
     a = ap.parse_args()
     from . import build
     build.build()
-    print(json.dumps(interface_problem_check(a.n, a.steps, a.stride, a.dirs)))
+    print(json.dumps(interface_problem_check(a.n, a.steps, a.stride, a.dirs, step_rho=a.step_rho,
+                                             step_eos=a.step_eos, background=a.background)))

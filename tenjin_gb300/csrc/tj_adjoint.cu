@@ -19,9 +19,22 @@
 //   k_adj_gather per cell: adjoint of the stage input (identity, the
 //                non-conservative alpha term, the MUSCL and THINC stencils,
 //                ghost images folded back onto their source cells)
-// Discrete choices are held at their forward values; alpha values taken from
-// the THINC scratch of earlier stages (the reference's stale ULStar/URStar
-// reads) are constants of the step.
+// Discrete choices are held at their forward values. Alpha values that the
+// BVD step takes from the THINC scratch (the reference's stale ULStar/URStar,
+// thinc.cpp:138-147,164-165, hllc.cpp:622-623) carry their adjoint back to
+// the pass that wrote them, through two adjoint slots per material and cell
+// that persist across stages, steps and checkpoint intervals:
+//   ULStar is rewritten by every flux pass with the star alpha of the upwind
+//   face state (hllc.cpp:406,419-468), so a value read in pass P was written
+//   by pass P - 1: k_adj_face adds the slot to that face state's alpha
+//   adjoint and clears it;
+//   URStar is written only by the THINC right candidate of a mixed cell, so a
+//   value read in pass P was written by the last earlier pass in which the
+//   cell was mixed: k_adj_thinc adds the slot to the candidate's adjoint there
+//   and clears it.
+// The reads of a pass are added to the slots (k_adj_scratch) after its
+// writes were reversed, and the two directions of a stage are reversed in the
+// order d = 1, then d = 0.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -221,7 +234,8 @@ __global__ void __launch_bounds__(NT) k_adj_c2p(AG G, const double* lamY, const 
 // Per face along d: adjoint of the two reconstructed states that meet there.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(NT) k_adj_face(AG G, int d, const double* X, const double* rec, const double* mu,
-                                                 double* lface, double* limg, double* sstar, double dt, double* gpart)
+                                                 double* lface, double* limg, double* sstar, double dt, double* gpart,
+                                                 double* sul)
 {
     const int M = G.M, NW = G.NW;
     const long long N = G.N;
@@ -276,6 +290,20 @@ __global__ void __launch_bounds__(NT) k_adj_face(AG G, int d, const double* X, c
         tja::zero(lL);
         tja::zero(lR);
         const double Ss = tja::hllc_rev(M, L, R, d, lF, lL, lR);
+        if (sul && hasR) {
+            // this pass wrote the star alpha of the face's upwind state into
+            // ULStar at its valid right cell (hllc.cpp:406,419-468): the
+            // adjoint that later reads of that slot gathered goes to it
+            const double x1 = fabs(L.u[d]) + L.c, x2 = fabs(R.u[d]) + R.c;
+            const double SL = -((x1 < x2) ? x2 : x1);
+            const bool left = (SL >= 0.0) || (Ss >= 0.0);
+            for (int m = 0; m < M; ++m) {
+                const double v = sul[(long long)m * N + gR];
+                if (left) lL.a[m] += v;
+                else lR.a[m] += v;
+                sul[(long long)m * N + gR] = 0.0;
+            }
+        }
         tja::Prim pL, pR;
         tja::zero(pL);
         tja::zero(pR);
@@ -302,7 +330,58 @@ __device__ double thinc_exp(double x) { return tjm_exp(x); }
 // Per cell along d: stencil gradient of each THINC candidate the forward used.
 // ---------------------------------------------------------------------------
 __global__ void k_adj_thinc(AG G, int d, const double* X, const int* code, const double* lface, const double* limg,
-                            double* tcon)
+                            double* tcon, double* sur)
+{
+    const int M = G.M, NW = G.NW;
+    const long long N = G.N;
+    const int n = d == 0 ? G.nx : G.ny;
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < N; g += (long long)gridDim.x * blockDim.x) {
+        const int cd = code[(long long)d * N + g];
+        const int i = (int)(g % G.nx), j = (int)(g / G.nx);
+        const int pos = d == 0 ? i : j, line = d == 0 ? j : i;
+        for (int m = 0; m < M; ++m) {
+            double* tc = tcon + (long long)((d * M + m) * 9) * N + g;
+            double s[3][3], ls[3][3];
+            for (int a = 0; a < 3; ++a)
+                for (int c = 0; c < 3; ++c) {
+                    bool r0, r1;
+                    const int ii = mapi(i + a - 1, G.nx, G.lo_bc[0], G.hi_bc[0], r0);
+                    const int jj = mapi(j + c - 1, G.ny, G.lo_bc[1], G.hi_bc[1], r1);
+                    s[a][c] = X[(G.sa + m) * N + ii + (long long)G.nx * jj];
+                    ls[a][c] = 0.0;
+                }
+            double cL = 0.0, cR = 0.0;
+            const bool mixed = tja::thinc_cand_fwd(s, d, G.beta, G.dx[0], G.dx[1], thinc_cosh, thinc_tanh, thinc_exp,
+                                                   cL, cR);
+            double lL = 0.0, lR = 0.0;
+            if (((cd >> (2 * m)) & 3) == 1) {  // the cell's own candidate, used in this pass
+                lL = lface[((long long)(d * 2) * NW + m) * N + g];
+                lR = lface[((long long)(d * 2 + 1) * NW + m) * N + g];
+                if (pos == n - 1) lL += limg[((long long)(d * 2 + 1) * NW + m) * G.nl + line];
+                if (pos == 0) lR += limg[((long long)(d * 2) * NW + m) * G.nl + line];
+            }
+            if (mixed && sur) {
+                // this pass wrote the right candidate into URStar
+                // (thinc.cpp:138-147): the adjoint of its later reads
+                lR += sur[(long long)m * N + g];
+                sur[(long long)m * N + g] = 0.0;
+            }
+            if (mixed && (lL != 0.0 || lR != 0.0))
+                tja::thinc_cand_rev(s, d, G.beta, G.dx[0], G.dx[1], thinc_cosh, thinc_tanh, thinc_exp, lL, lR, ls);
+            for (int a = 0; a < 3; ++a)
+                for (int c = 0; c < 3; ++c) tc[(long long)(a * 3 + c) * N] = ls[a][c];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Per cell along d: the reconstructed alpha values this pass took from the
+// THINC scratch (code 2: UL alpha = ULStar, UR alpha = URStar of the cell)
+// add their adjoint to the scratch slots, for the earlier passes that wrote
+// those values.
+// ---------------------------------------------------------------------------
+__global__ void k_adj_scratch(AG G, int d, const int* code, const double* lface, const double* limg, double* sul,
+                              double* sur)
 {
     const int M = G.M, NW = G.NW;
     const long long N = G.N;
@@ -313,23 +392,13 @@ __global__ void k_adj_thinc(AG G, int d, const double* X, const int* code, const
         const int i = (int)(g % G.nx), j = (int)(g / G.nx);
         const int pos = d == 0 ? i : j, line = d == 0 ? j : i;
         for (int m = 0; m < M; ++m) {
-            if (((cd >> (2 * m)) & 3) != 1) continue;
+            if (((cd >> (2 * m)) & 3) != 2) continue;
             double lL = lface[((long long)(d * 2) * NW + m) * N + g];
             double lR = lface[((long long)(d * 2 + 1) * NW + m) * N + g];
             if (pos == n - 1) lL += limg[((long long)(d * 2 + 1) * NW + m) * G.nl + line];
             if (pos == 0) lR += limg[((long long)(d * 2) * NW + m) * G.nl + line];
-            double s[3][3], ls[3][3];
-            for (int a = 0; a < 3; ++a)
-                for (int c = 0; c < 3; ++c) {
-                    bool r0, r1;
-                    const int ii = mapi(i + a - 1, G.nx, G.lo_bc[0], G.hi_bc[0], r0);
-                    const int jj = mapi(j + c - 1, G.ny, G.lo_bc[1], G.hi_bc[1], r1);
-                    s[a][c] = X[(G.sa + m) * N + ii + (long long)G.nx * jj];
-                    ls[a][c] = 0.0;
-                }
-            tja::thinc_cand_rev(s, d, G.beta, G.dx[0], G.dx[1], thinc_cosh, thinc_tanh, thinc_exp, lL, lR, ls);
-            for (int a = 0; a < 3; ++a)
-                for (int c = 0; c < 3; ++c) tcon[((long long)((d * M + m) * 9) + a * 3 + c) * N + g] = ls[a][c];
+            sul[(long long)m * N + g] += lL;
+            sur[(long long)m * N + g] += lR;
         }
     }
 }
@@ -396,10 +465,9 @@ __global__ void __launch_bounds__(NT) k_adj_gather(AG G, const double* X, const 
                         const int ci = i + a, cj = j + c;
                         if (ci < 0 || ci >= G.nx || cj < 0 || cj >= G.ny) continue;
                         const long long gi = ci + (long long)G.nx * cj;
-                        const int cd = code[(long long)d * N + gi];
-                        if (!cd) continue;
                         for (int m = 0; m < M; ++m) {
-                            if (((cd >> (2 * m)) & 3) != 1) continue;
+                            // k_adj_thinc wrote every cell's slots (zero where
+                            // no candidate of this pass carries an adjoint)
                             for (int oa = 0; oa < 3; ++oa)
                                 for (int oc = 0; oc < 3; ++oc) {
                                     bool r0, r1;
@@ -537,6 +605,7 @@ struct AdjState {
     int* code = nullptr;
     double *lam = nullptr, *lamA = nullptr, *lamB = nullptr, *mu = nullptr, *lface = nullptr, *limg = nullptr;
     double *sstar = nullptr, *tcon = nullptr, *gpart = nullptr, *gsum = nullptr;
+    double *sul = nullptr, *sur = nullptr;  // adjoint of the ULStar / URStar alpha slots
     size_t bytes = 0;
     size_t cap_ck = 0, cap_seg = 0;  // allocated checkpoint / interval capacity (in checkpoints, in steps)
     long long capN = -1;
@@ -560,12 +629,13 @@ AdjState* adj_create() { return new AdjState(); }
 static void free_all(AdjState* a)
 {
     double* ds[] = {a->ck, a->seg, a->rec, a->lam, a->lamA, a->lamB, a->mu, a->lface, a->limg, a->sstar, a->tcon,
-                    a->gpart, a->gsum};
+                    a->gpart, a->gsum, a->sul, a->sur};
     for (double* p : ds)
         if (p) cudaFree(p);
     if (a->code) cudaFree(a->code);
     a->ck = a->seg = a->rec = a->lam = a->lamA = a->lamB = a->mu = a->lface = a->limg = a->sstar = a->tcon = nullptr;
     a->gpart = a->gsum = nullptr;
+    a->sul = a->sur = nullptr;
     a->code = nullptr;
     a->bytes = 0;
     a->cap_ck = a->cap_seg = 0;
@@ -609,7 +679,7 @@ static int ensure(AdjState* a, const DevParams& P, const Fp64Bufs& b, const DevD
               dalloc(a, &a->lamB, (size_t)ns * N) && dalloc(a, &a->mu, NW * N) && dalloc(a, &a->lface, 4 * NW * N) &&
               dalloc(a, &a->limg, 4 * NW * nl) && dalloc(a, &a->sstar, nf0 + nf1) &&
               dalloc(a, &a->tcon, (size_t)2 * M * 9 * N) && dalloc(a, &a->gpart, (size_t)NBLK * NG) &&
-              dalloc(a, &a->gsum, NG);
+              dalloc(a, &a->gsum, NG) && dalloc(a, &a->sul, (size_t)M * N) && dalloc(a, &a->sur, (size_t)M * N);
     if (!ok) {
         free_all(a);
         return TJ_ERR_CUDA;
@@ -689,6 +759,8 @@ long long adj_backward(AdjState* a, const DevParams& P, const Fp64Bufs& b, const
     long long launches = 0;
     cudaMemcpyAsync(a->lam, lam_final, sizeof(double) * sw, cudaMemcpyDeviceToDevice, st);
     cudaMemsetAsync(a->gpart, 0, sizeof(double) * NBLK * NG, st);
+    cudaMemsetAsync(a->sul, 0, sizeof(double) * M * N, st);
+    cudaMemsetAsync(a->sur, 0, sizeof(double) * M * N, st);
     auto S = [&](int k, int which) { return a->seg + (size_t)(3 * k + which) * sw; };
     const size_t recw = (size_t)4 * M * N;
     for (int s = a->nck - 1; s >= 0; --s) {
@@ -721,13 +793,18 @@ long long adj_backward(AdjState* a, const DevParams& P, const Fp64Bufs& b, const
                 const double* rec = a->rec + (size_t)(2 * k + stage) * recw;
                 const int* code = a->code + (size_t)(2 * k + stage) * 2 * N;
                 k_adj_c2p<<<NBLK, NT, 0, st>>>(G, lamY, Y, a->mu, a->gpart);
-                for (int d = 0; d < 2; ++d)
-                    k_adj_face<<<NBLK, NT, 0, st>>>(G, d, X, rec, a->mu, a->lface, a->limg,
-                                                    a->sstar + (d ? nf0 : 0), dtn, a->gpart);
-                launches += 3;
-                if (P.thinc) {
-                    for (int d = 0; d < 2; ++d) k_adj_thinc<<<nb(N), NT, 0, st>>>(G, d, X, code, a->lface, a->limg, a->tcon);
-                    launches += 2;
+                launches += 1;
+                // the stage's passes in reverse order (d = 1, then d = 0): each
+                // pass's scratch writes are reversed before its reads
+                for (int d = 1; d >= 0; --d) {
+                    k_adj_face<<<NBLK, NT, 0, st>>>(G, d, X, rec, a->mu, a->lface, a->limg, a->sstar + (d ? nf0 : 0),
+                                                    dtn, a->gpart, P.thinc ? a->sul : nullptr);
+                    launches += 1;
+                    if (P.thinc) {
+                        k_adj_thinc<<<nb(N), NT, 0, st>>>(G, d, X, code, a->lface, a->limg, a->tcon, a->sur);
+                        k_adj_scratch<<<nb(N), NT, 0, st>>>(G, d, code, a->lface, a->limg, a->sul, a->sur);
+                        launches += 2;
+                    }
                 }
                 k_adj_gather<<<nb(N), NT, 0, st>>>(G, X, code, a->lface, a->limg, a->mu, a->sstar, a->sstar + nf0,
                                                    a->tcon, lamX, dtn, stage == 0 ? 1 : 0);

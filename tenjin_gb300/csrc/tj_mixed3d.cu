@@ -96,14 +96,19 @@ struct Sm3 {
     static constexpr int SX = TX + 4, SY = TY + 4, SZ = TZ + 4;
     static constexpr int SV = SX * SY * SZ;  // staged cells
     static constexpr int CV = TX * TY * TZ;  // output cells
-    static constexpr int FV = cmax(cmax((TX + 1) * TY * TZ, TX * (TY + 1) * TZ), TX * TY * (TZ + 1));
+    // faces of each direction (x faces, y faces, z faces of the tile)
+    static constexpr int FV0 = (TX + 1) * TY * TZ, FV1 = TX * (TY + 1) * TZ, FV2 = TX * TY * (TZ + 1);
     static constexpr int NP = 2 * M + 4;  // staged primitives: alpha[M], rho_k[M], u[3], p
     static constexpr int NC = 2 * M + 5;  // conserved: alpha[M], alphaRho[M], rhoU[3], E hi, E lo
     static constexpr int NF = 2 * M + 5;  // face flux: alpha[M], alphaRho[M], rhoU[3], E, S*
     static constexpr int P_OFF = 0;
     static constexpr int C_OFF = P_OFF + NP * SV;
+    // the face fluxes of all three directions at once: word q of direction d
+    // at F_OFF + FD(d) + q * FVd(d) + face
     static constexpr int F_OFF = C_OFF + NC * CV;
-    static constexpr int RED_OFF = F_OFF + NF * FV;
+    static constexpr int RED_OFF = F_OFF + NF * (FV0 + FV1 + FV2);
+    static __host__ __device__ constexpr int FVd(int d) { return d == 0 ? FV0 : (d == 1 ? FV1 : FV2); }
+    static __host__ __device__ constexpr int FD(int d) { return d == 0 ? 0 : (d == 1 ? NF * FV0 : NF * (FV0 + FV1)); }
     static constexpr int TOTAL = RED_OFF + 64;
     // a second staging buffer (primitives and conserved words) after TOTAL:
     // the next tile's copies land there while this tile computes
@@ -424,69 +429,80 @@ __global__ void __launch_bounds__(NT3) k_stage3d(M3P P, M3B b, int stage, int fo
         const long long off = D.off;
         const int nx = D.n[0], ny = D.n[1], nz = D.n[2];
 
+        // ---- faces of all three directions: the update is unsplit, so every
+        //      face reads the same staged stage-input state; the faces are dealt
+        //      to the threads round-robin over the three directions' list, so
+        //      that no thread waits for a second round that only a few need ----
+        {
+            int base = 0;
 #pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            const int fx = ex + (d == 0), fy = ey + (d == 1), fz = ez + (d == 2);
-            const int stride = d == 0 ? 1 : (d == 1 ? SM::SX : SM::SX * SM::SY);
-            const int n_d = d == 0 ? nx : (d == 1 ? ny : nz);
-            const int p0 = d == 0 ? i0 : (d == 1 ? j0 : k0);
-            const bool lo_refl = P.lo_bc[d] == TJ_BC_REFLECTIVE, hi_refl = P.hi_bc[d] == TJ_BC_REFLECTIVE;
-            // ---- faces ----
-            for (int t = threadIdx.x; t < fx * fy * fz; t += NT3) {
-                const int x = t % fx, y = (t / fx) % fy, z = t / (fx * fy);
-                const int f_d = d == 0 ? x : (d == 1 ? y : z);
-                const int posR = p0 + f_d;  // the face's right cell along d
-                // staged index of the right cell and the left cell
-                const int sR = (x + 2) + SM::SX * ((y + 2) + SM::SY * (z + 2));
-                const int sL = sR - stride;
-                FS3<M> L, R;
-                if (posR == 0) recon3<M, TX, TY, TZ>(P, sp, sR, stride, 1, d, lo_refl, L);  // image of UR(0)
-                else recon3<M, TX, TY, TZ>(P, sp, sL, stride, 1, d, false, L);
-                if (posR == n_d) recon3<M, TX, TY, TZ>(P, sp, sL, stride, 0, d, hi_refl, R);  // image of UL(n-1)
-                else recon3<M, TX, TY, TZ>(P, sp, sR, stride, 0, d, false, R);
-                float F[2 * M + 5];
-                hllc3<M>(L, R, d, F);
-                const int fidx = x + fx * (y + fy * z);
+            for (int d = 0; d < 3; ++d) {
+                const int fx = ex + (d == 0), fy = ey + (d == 1), fz = ez + (d == 2);
+                const int nfd = fx * fy * fz;
+                const int stride = d == 0 ? 1 : (d == 1 ? SM::SX : SM::SX * SM::SY);
+                const int n_d = d == 0 ? nx : (d == 1 ? ny : nz);
+                const int p0 = d == 0 ? i0 : (d == 1 ? j0 : k0);
+                const bool lo_refl = P.lo_bc[d] == TJ_BC_REFLECTIVE, hi_refl = P.hi_bc[d] == TJ_BC_REFLECTIVE;
+                int u0 = ((int)threadIdx.x - base) % NT3;
+                if (u0 < 0) u0 += NT3;
+                for (int t = u0; t < nfd; t += NT3) {
+                    const int x = t % fx, y = (t / fx) % fy, z = t / (fx * fy);
+                    const int f_d = d == 0 ? x : (d == 1 ? y : z);
+                    const int posR = p0 + f_d;  // the face's right cell along d
+                    // staged index of the right cell and the left cell
+                    const int sR = (x + 2) + SM::SX * ((y + 2) + SM::SY * (z + 2));
+                    const int sL = sR - stride;
+                    FS3<M> L, R;
+                    if (posR == 0) recon3<M, TX, TY, TZ>(P, sp, sR, stride, 1, d, lo_refl, L);  // image of UR(0)
+                    else recon3<M, TX, TY, TZ>(P, sp, sL, stride, 1, d, false, L);
+                    if (posR == n_d) recon3<M, TX, TY, TZ>(P, sp, sL, stride, 0, d, hi_refl, R);  // image of UL(n-1)
+                    else recon3<M, TX, TY, TZ>(P, sp, sR, stride, 0, d, false, R);
+                    float F[2 * M + 5];
+                    hllc3<M>(L, R, d, F);
+                    const int fidx = x + fx * (y + fy * z);
 #pragma unroll
-                for (int q = 0; q < 2 * M + 5; ++q) sm[SM::F_OFF + q * SM::FV + fidx] = F[q];
+                    for (int q = 0; q < 2 * M + 5; ++q) sm[SM::F_OFF + SM::FD(d) + q * SM::FVd(d) + fidx] = F[q];
+                }
+                base += nfd;
             }
-            __syncthreads();
-            // ---- update ----
-            const float dtdx = dtf * D.idx[d];
-            for (int t = threadIdx.x; t < ex * ey * ez; t += NT3) {
-                const int x = t % ex, y = (t / ex) % ey, z = t / (ex * ey);
+        }
+        __syncthreads();
+
+        // ---- per cell: the update of the three directions in order x, y, z
+        //      (hllc.cpp:493-523), then the finish; a cell's words are touched
+        //      by its own thread only, so no barrier separates the two ----
+        for (int t = threadIdx.x; t < ex * ey * ez; t += NT3) {
+            const int x = t % ex, y = (t / ex) % ey, z = t / (ex * ey);
+            const int c = x + TX * (y + TY * z);
+            const int s = (x + 2) + SM::SX * ((y + 2) + SM::SY * (z + 2));
+            float* C = sp + SM::C_OFF;
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                const int fx = ex + (d == 0), fy = ey + (d == 1);
                 const int f0 = x + fx * (y + fy * z);
                 const int f1 = f0 + (d == 0 ? 1 : (d == 1 ? fx : fx * fy));
-                const int c = x + TX * (y + TY * z);
-                const int s = (x + 2) + SM::SX * ((y + 2) + SM::SY * (z + 2));
-                const float* Fl = sm + SM::F_OFF;
-                const float dS = Fl[(2 * M + 4) * SM::FV + f0] - Fl[(2 * M + 4) * SM::FV + f1];
-                float* C = sp + SM::C_OFF;
+                const float dtdx = dtf * D.idx[d];
+                const float* Fl = sm + SM::F_OFF + SM::FD(d);
+                const int fv = SM::FVd(d);
+                const float dS = Fl[(2 * M + 4) * fv + f0] - Fl[(2 * M + 4) * fv + f1];
 #pragma unroll
                 for (int m = 0; m < M; ++m) {
                     const float a0 = sp[SM::P_OFF + m * SM::SV + s];
-                    C[m * SM::CV + c] += dtdx * (Fl[m * SM::FV + f0] - Fl[m * SM::FV + f1] - a0 * dS);
-                    C[(M + m) * SM::CV + c] += dtdx * (Fl[(M + m) * SM::FV + f0] - Fl[(M + m) * SM::FV + f1]);
+                    C[m * SM::CV + c] += dtdx * (Fl[m * fv + f0] - Fl[m * fv + f1] - a0 * dS);
+                    C[(M + m) * SM::CV + c] += dtdx * (Fl[(M + m) * fv + f0] - Fl[(M + m) * fv + f1]);
                 }
 #pragma unroll
                 for (int r = 0; r < 3; ++r)
-                    C[(2 * M + r) * SM::CV + c] +=
-                        dtdx * (Fl[(2 * M + r) * SM::FV + f0] - Fl[(2 * M + r) * SM::FV + f1]);
+                    C[(2 * M + r) * SM::CV + c] += dtdx * (Fl[(2 * M + r) * fv + f0] - Fl[(2 * M + r) * fv + f1]);
                 float eh = C[(2 * M + 3) * SM::CV + c], el = C[(2 * M + 4) * SM::CV + c];
-                dd_add3(eh, el, dtdx * (Fl[(2 * M + 3) * SM::FV + f0] - Fl[(2 * M + 3) * SM::FV + f1]));
+                dd_add3(eh, el, dtdx * (Fl[(2 * M + 3) * fv + f0] - Fl[(2 * M + 3) * fv + f1]));
                 C[(2 * M + 3) * SM::CV + c] = eh;
                 C[(2 * M + 4) * SM::CV + c] = el;
             }
-            __syncthreads();
-        }
 
-        // ---- finish ----
-        for (int t = threadIdx.x; t < ex * ey * ez; t += NT3) {
-            const int x = t % ex, y = (t / ex) % ey, z = t / (ex * ey);
+            // ---- finish ----
             const int gi = i0 + x, gj = j0 + y, gk = k0 + z;
             const long long g = off + gi + (long long)nx * (gj + (long long)ny * gk);
-            const int c = x + TX * (y + TY * z);
-            const float* C = sp + SM::C_OFF;
             float a[M], ar[M], rk[M], ru[3], u[3], eh, el, p;
 #pragma unroll
             for (int m = 0; m < M; ++m) {
@@ -732,9 +748,18 @@ void stage_launch(const M3P& P, const M3B& b, int stage, int force, int grid, si
 template <int M, int TX, int TY, int TZ>
 int stage_occupancy(size_t smem)
 {
-    cudaFuncSetAttribute(k_stage3d<M, TX, TY, TZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    // a shape whose shared memory exceeds the opt-in maximum cannot run here:
+    // 0, with the error the attribute call raised cleared
+    if (cudaFuncSetAttribute(k_stage3d<M, TX, TY, TZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
     int nb = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_stage3d<M, TX, TY, TZ>, NT3, smem);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_stage3d<M, TX, TY, TZ>, NT3, smem) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
     return nb;
 }
 
@@ -787,6 +812,7 @@ struct Mixed3D : MixedBase {
     Dom3* d_doms = nullptr;
     Work3* d_work = nullptr;  // every tile of every class (the CFL pass)
     std::vector<Shape> cand;
+    std::vector<int> occ;  // resident CTAs per SM of each candidate (0: does not fit)
     ClassPlan cls[kClasses];
     bool tuned = false;
     int sms = 0;
@@ -840,6 +866,8 @@ struct Mixed3D : MixedBase {
         int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        occ.clear();
+        for (const Shape& S : cand) occ.push_back(S.occupancy(S.smem));
         b.X[0] = X[0];
         b.X[1] = X[1];
         b.N = N;
@@ -892,17 +920,27 @@ struct Mixed3D : MixedBase {
         return TJ_OK;
     }
 
+    // Whether shape s fits this GPU at this material count (its shared
+    // memory at most the opt-in maximum): at least one resident CTA.
+    bool fits(int s) const { return occ[s] >= 1; }
+
+    int first_fit() const
+    {
+        for (size_t s = 0; s < cand.size(); ++s)
+            if (fits((int)s)) return (int)s;
+        return -1;
+    }
+
     // Class c's work list under shape s, on the device, and its grid.
     int plan_class(int c, int s, cudaStream_t st)
     {
+        if (s < 0 || !fits(s)) return TJ_ERR_ARG;
         ClassPlan& C = cls[c];
         const std::vector<Work3> w = tiles(C.doms, s);
         if (int e = upload(C.d_work, w, st)) return e;
         C.nwork = (int)w.size();
         C.best = s;
-        const Shape& S = cand[s];
-        const int occ = std::max(1, S.occupancy(S.smem));
-        C.grid = std::max(1, std::min(C.nwork, sms * occ));
+        C.grid = std::max(1, std::min(C.nwork, sms * occ[s]));
         return TJ_OK;
     }
 
@@ -912,7 +950,7 @@ struct Mixed3D : MixedBase {
         std::vector<Work3> all;
         for (int c = 0; c < kClasses; ++c) {
             if (cls[c].doms.empty()) continue;
-            const std::vector<Work3> w = tiles(cls[c].doms, std::max(0, cls[c].best));
+            const std::vector<Work3> w = tiles(cls[c].doms, cls[c].best >= 0 ? cls[c].best : std::max(0, first_fit()));
             all.insert(all.end(), w.begin(), w.end());
         }
         if (int e = upload(d_work, all, st)) return e;
@@ -961,9 +999,11 @@ struct Mixed3D : MixedBase {
         cudaMemcpyAsync(d_doms, d3.data(), sizeof(Dom3) * d3.size(), cudaMemcpyHostToDevice, st);
         b.doms = d_doms;
         tuned = false;  // re-tune on the next upload
+        const int s0 = first_fit();
+        if (s0 < 0) return TJ_ERR_ARG;
         for (int c = 0; c < kClasses; ++c)
             if (!cls[c].doms.empty())
-                if (int e = plan_class(c, 0, st)) return e;
+                if (int e = plan_class(c, s0, st)) return e;
         return plan_all(st);
     }
 
@@ -987,13 +1027,10 @@ struct Mixed3D : MixedBase {
         for (int c = 0; c < kClasses; ++c) {
             ClassPlan& C = cls[c];
             if (C.doms.empty()) continue;
-            if (pinned >= 0) {
-                plan_class(c, pinned, st);
-                continue;
-            }
+            if (pinned >= 0 && plan_class(c, pinned, st) == TJ_OK) continue;
             C.tune_ms.assign(cand.size(), 0.0);
             float bestms = 3e38f;
-            int bi = 0;
+            int bi = first_fit();
             for (size_t s = 0; s < cand.size(); ++s) {
                 if (plan_class(c, (int)s, st) != TJ_OK) continue;
                 const M3B bc = class_bufs(c);
