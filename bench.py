@@ -496,7 +496,7 @@ def main():
     ap.add_argument("--accuracy-steps", type=int, default=2000, help="steps of the precision comparison")
     ap.add_argument("--no-other-configs", dest="other_configs", action="store_false",
                     help="skip the 3-D configurations")
-    ap.add_argument("--adjoint-dirs", type=int, default=8,
+    ap.add_argument("--adjoint-dirs", type=int, default=16,
                     help="finite-difference directions of the adjoint check (-1: skip the adjoint)")
     ap.add_argument("--no-fp64-compare", dest="fp64_compare", action="store_false")
     ap.add_argument("--e2e-steps", type=int, default=10)

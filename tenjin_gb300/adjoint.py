@@ -138,7 +138,7 @@ def density_misfit(state: torch.Tensor, target: torch.Tensor, M: int, cell_area:
 
 
 def interface_problem_check(n: int = 512, nsteps: int = 200, stride: int = 20, ndir: int = 64,
-                            step_rho: float = 1e-8, step_eos: float = 1e-6, seed: int = 0,
+                            step_rho: float = 1e-8, step_eos: float = 1e-8, seed: int = 0,
                             background: float = 1e-3) -> dict:
     """The adjoint on the 2-D water/air interface problem: n^2 cells, nsteps
     steps with the dt schedule of a plain FP64 run, checkpoints every
@@ -151,9 +151,12 @@ def interface_problem_check(n: int = 512, nsteps: int = 200, stride: int = 20, n
     smooth background of relative amplitude `background` (the limiter has no
     derivative at an exactly uniform state). Each direction is checked as the
     sum of its two parts, each differenced with its own relative step:
-    `step_rho` along the partial densities (finite differences straddle
-    limiter kinks there, an error that falls with the step) and `step_eos`
-    along the EOS parameters (smooth; smaller steps only add rounding)."""
+    `step_rho` along the partial densities and `step_eos` along the EOS
+    parameters. Along both, central differences straddle the kinks of the
+    discrete choices (limiter, BVD-THINC, wave-speed maxima, HLLC side) of
+    cells whose margin is below the step, an error that falls with the step:
+    at 128^2 and 60 steps the EOS part goes from 4e-5 at 1e-6 to 3e-6 at 1e-8
+    while rounding stays below 1e-6."""
     import time
 
     from . import cases
@@ -231,7 +234,7 @@ if __name__ == "__main__":
     ap.add_argument("--stride", type=int, default=20)
     ap.add_argument("--dirs", type=int, default=64)
     ap.add_argument("--step-rho", type=float, default=1e-8, help="relative step along the partial densities")
-    ap.add_argument("--step-eos", type=float, default=1e-6, help="relative step along (gamma, p_ref)")
+    ap.add_argument("--step-eos", type=float, default=1e-8, help="relative step along (gamma, p_ref)")
     ap.add_argument("--background", type=float, default=1e-3,
                     help="relative amplitude of the smooth background of the base state (0: the configuration as "
                          "stated, with exactly uniform regions)")
