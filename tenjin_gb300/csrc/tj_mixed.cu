@@ -829,6 +829,22 @@ __global__ void __launch_bounds__(NTH, sizeof(R) == 4 ? 3 : 1) k_stage2d(MixP<R>
         cp_async_r(Sc + (2 * M + 3) * SM::CT, Xin + W_EL<M>() * N + g);
     }
     asm volatile("cp.async.commit_group;\n" ::: "memory");
+    if (stage == 1) {
+        // The second stage's finish averages with U^n (hllc.cpp:705), which
+        // the first stage's output has mostly pushed out of L2: ask for the
+        // output cells' rows of every U^n word now, so that they arrive
+        // while the sweeps run (both ends of each 28-cell row, which may
+        // span two 128-byte lines).
+        constexpr int NW = NWORDS<M>();
+        for (int t = threadIdx.x; t < NW * MT * 2; t += NTH) {
+            const int w = t / (2 * MT), r = (t >> 1) % MT, e = t & 1;
+            const int gx = min(x0 + e * (MT - 1), P.nx - 1), gy = y0 + r;
+            if (gy < P.ny) {
+                const R* a = Xout + (long long)w * N + gx + (long long)P.nx * gy;
+                asm volatile("prefetch.global.L2 [%0];\n" ::"l"(a));
+            }
+        }
+    }
     asm volatile("cp.async.wait_group 0;\n" ::: "memory");
     __syncthreads();
     // reflect_odd ghosts (FillDomainBoundary): negate the normal velocity of
