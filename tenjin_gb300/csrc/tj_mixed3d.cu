@@ -351,6 +351,22 @@ __device__ void stage_issue(const M3P& P, const Work3& w, const Dom3& D, const f
     }
 }
 
+// The second stage's finish averages with U^n (hllc.cpp:705): ask L2 for the
+// rows of a tile's output cells in every U^n word when the tile's staging is
+// queued, so that they arrive while the tile before it computes.
+template <int M>
+__device__ __forceinline__ void prefetch_un(const Work3& w, const Dom3& D, const float* __restrict__ Xun, long long N)
+{
+    const int ey = w.ey, ez = w.ez, ex = w.ex;
+    const int nrow = ey * ez;
+    for (int t = threadIdx.x; t < S3_N<M>() * nrow * 2; t += NT3) {
+        const int q = t / (2 * nrow), r = (t >> 1) % nrow, e = t & 1;
+        const int y = r % ey, z = r / ey;
+        const long long g = D.off + (w.i0 + e * (ex - 1)) + (long long)D.n[0] * ((w.j0 + y) + (long long)D.n[1] * (w.k0 + z));
+        asm volatile("prefetch.global.L2 [%0];\n" ::"l"(Xun + (long long)q * N + g));
+    }
+}
+
 // The reflect_odd ghosts (FillDomainBoundary) of a landed staging buffer:
 // negate the velocity normal to each reflective face the ghost crosses.
 // Returns whether the tile reaches a reflective face (the same answer in
@@ -405,6 +421,7 @@ __global__ void __launch_bounds__(NT3) k_stage3d(M3P P, M3B b, int stage, int fo
         }
         __syncthreads();
         stage_issue<M, TX, TY, TZ>(P, wsh[0], Dsh[0], Xin, N, sm);
+        if (stage == 1) prefetch_un<M>(wsh[0], Dsh[0], Xout, N);
     }
     cp_async_commit();
     for (int it = 0; wi < b.nwork; wi += gridDim.x, ++it) {
@@ -417,7 +434,10 @@ __global__ void __launch_bounds__(NT3) k_stage3d(M3P P, M3B b, int stage, int fo
             Dsh[nxt] = b.doms[wsh[nxt].dom];
         }
         __syncthreads();
-        if (wn < b.nwork) stage_issue<M, TX, TY, TZ>(P, wsh[nxt], Dsh[nxt], Xin, N, sm + (nxt ? SM::TOTAL : 0));
+        if (wn < b.nwork) {
+            stage_issue<M, TX, TY, TZ>(P, wsh[nxt], Dsh[nxt], Xin, N, sm + (nxt ? SM::TOTAL : 0));
+            if (stage == 1) prefetch_un<M>(wsh[nxt], Dsh[nxt], Xout, N);
+        }
         cp_async_commit();
         cp_async_wait<1>();  // this tile's copies have landed
         __syncthreads();
