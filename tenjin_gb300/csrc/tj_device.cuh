@@ -592,6 +592,16 @@ __device__ __forceinline__ void closure_terms64(const P32& P, int m, const ECell
     }
 }
 
+// (sh, sl) += b: the rounding error of sh + b (Knuth's two-sum, every
+// operation rounded to nearest) is added to the low word.
+__device__ __forceinline__ void acc_pair32(float& sh, float& sl, float b)
+{
+    const float s = __fadd_rn(sh, b);
+    const float bb = __fsub_rn(s, sh);
+    sl = __fadd_rn(sl, __fadd_rn(__fsub_rn(sh, __fsub_rn(s, bb)), __fsub_rn(b, bb)));
+    sh = s;
+}
+
 // conservativeToPrimitive (:67-122). Returns 0, or TJ_ERR_ROOT from the
 // mixture closure.
 template <typename PT>
@@ -613,9 +623,23 @@ __device__ __forceinline__ int c2p(const PT& P, CellT<typename PT::real>& c)
         ke += R(0.5) * c.rho * c.vel[r] * c.vel[r];
     }
     if constexpr (sizeof(R) == 4) {
-        // binary32 state: the closure of the pressure (and of the mixture
-        // densities) in binary64, from the compensated energy (E, Elo) and
-        // binary64 cold terms
+        if (P.M == 1 && !P.nmix) {
+            // one material: no interface whose stiff cold terms cancel the
+            // energy, so the closure stays binary32, with the numerator
+            // E + Elo - KE - e_cold + p_cold summed without rounding error
+            // into an unevaluated pair (error-free sums)
+            const R ent = eff_e_nonthermal(P, c), pnt = eff_p_nonthermal(P, c), ig = eff_invG(P, c);
+            R sh = c.E, sl = c.Elo;
+            acc_pair32(sh, sl, -ke);
+            acc_pair32(sh, sl, -ent);
+            acc_pair32(sh, sl, pnt);
+            c.p = __fadd_rn(sh, sl) / ig;
+            stress(P, c);
+            return err;
+        }
+        // binary32 state with several materials: the closure of the pressure
+        // (and of the mixture densities) in binary64, from the compensated
+        // energy (E, Elo) and binary64 cold terms
         double rho = 0.0, ent = 0.0, pnt = 0.0, ig = 0.0;
         for (int m = 0; m < P.M; ++m) rho += (double)c.arho[m];
         const double ru0 = c.rhou[0], ru1 = c.rhou[1], ru2 = c.rhou[2];
