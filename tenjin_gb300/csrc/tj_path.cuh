@@ -248,6 +248,76 @@ __device__ inline void load_face(const PT& P, const R* F, long long nt, long lon
     if (P.nmix) c.arl = F[P.F_ARL * nt + g];
 }
 
+// Without BVD-THINC (whose repeated cleanUpAlpha feeds the closures one
+// alpha and the flux another) and without mixtures, the reconstruction
+// stores the primitives of each face state -- alpha[M], rho_k[M], u[3], p,
+// V[9] (solids), epsilon[M] (plastic): 16 words for the copper plate instead
+// of the 31 of a closed state -- and the flux kernel closes them
+// (primitiveToConservative, getSoundSpeed) where it reads them: the same
+// calls on the same values, so the same bits reach the Riemann solver.
+template <typename PT>
+__device__ __forceinline__ bool compact_faces(const PT& P)
+{
+    return !P.thinc && !P.nmix;
+}
+
+template <typename PT, typename R = typename PT::real>
+__device__ inline void store_prim_face(const PT& P, R* F, long long nt, long long g, const CellT<R>& c)
+{
+    int w = 0;
+    for (int m = 0; m < P.M; ++m) F[(long long)(w++) * nt + g] = c.alpha[m];
+    for (int m = 0; m < P.M; ++m) F[(long long)(w++) * nt + g] = c.rhok[m];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) F[(long long)(w++) * nt + g] = c.vel[r];
+    F[(long long)(w++) * nt + g] = c.p;
+    if (P.solid) {
+#pragma unroll
+        for (int q = 0; q < 9; ++q) F[(long long)(w++) * nt + g] = c.V[q];
+        if (!P.any_solid) F[(long long)(w++) * nt + g] = c.hj2;  // getHenckyJ2 does not run: the cell's own
+    }
+    if (P.plastic)  // epsilon of a solid closes alphaRhoEps; a fluid's alphaRhoEps is the cell's own
+        for (int m = 0; m < P.M; ++m) F[(long long)(w++) * nt + g] = P.phase[m] == TJ_PHASE_SOLID ? c.eps[m] : c.are[m];
+}
+
+// The closed face state of load_face from stored primitives: the closures
+// of the reconstruction, then the fields load_face leaves at zero, then the
+// reflect_odd sign of a boundary image.
+template <typename PT, typename R = typename PT::real>
+__device__ inline void load_prim_face(const PT& P, const R* F, long long nt, long long g, int oddir, CellT<R>& c)
+{
+    int w = 0;
+    for (int m = 0; m < P.M; ++m) c.alpha[m] = F[(long long)(w++) * nt + g];
+    for (int m = 0; m < P.M; ++m) c.rhok[m] = F[(long long)(w++) * nt + g];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) c.vel[r] = F[(long long)(w++) * nt + g];
+    c.p = F[(long long)(w++) * nt + g];
+    c.hj2 = R(0.0);
+    if (P.solid) {
+#pragma unroll
+        for (int q = 0; q < 9; ++q) c.V[q] = F[(long long)(w++) * nt + g];
+        if (!P.any_solid) c.hj2 = F[(long long)(w++) * nt + g];
+    }
+    if (P.plastic)
+        for (int m = 0; m < P.M; ++m) {
+            const R v = F[(long long)(w++) * nt + g];
+            if (P.phase[m] == TJ_PHASE_SOLID) c.eps[m] = v;
+            else c.are[m] = v;
+        }
+    p2c(P, c);
+    c.a = sound_speed(P, c);
+    for (int m = 0; m < P.M; ++m) c.rhok[m] = R(0.0);
+    c.hj2 = R(0.0);
+    if (!P.solid)
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+            for (int q = 0; q < 3; ++q) c.sigma[3 * r + q] = -c.p * (R)(r == q);  // stressTensor, fluid
+    if (oddir >= 0) {
+        c.vel[oddir] = -c.vel[oddir];
+        c.rhou[oddir] = -c.rhou[oddir];
+    }
+}
+
 template <typename R>
 __device__ __forceinline__ R vanleer(R r)  // hllc.cpp:527-537
 {
@@ -446,6 +516,11 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1)
                     b.ulstar[(long long)m * nt + g] = tc.L[m];
                     b.urstar[(long long)m * nt + g] = tc.Rv[m];
                 }
+        }
+        if (compact_faces(P)) {  // closed by the flux kernel
+            store_prim_face(P, b.UL, nt, g, L);
+            store_prim_face(P, b.UR, nt, g, Rc);
+            continue;
         }
         // cleanUpAlpha of UL and UR: nbox-b times for box b, the closures see
         // the first (hllc.cpp:628-638).
@@ -761,8 +836,13 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1) k_flux(PT P, Path
         long long gl = map_cell(P, D, i - o[0], j - o[1], k - o[2], rl);
         long long gr = map_cell(P, D, i, j, k, rr);
         CellT<R> L, Rc;
-        load_face(P, b.UR, nt, gl, rl[d] ? d : -1, L);
-        load_face(P, b.UL, nt, gr, rr[d] ? d : -1, Rc);
+        if (compact_faces(P)) {
+            load_prim_face(P, b.UR, nt, gl, rl[d] ? d : -1, L);
+            load_prim_face(P, b.UL, nt, gr, rr[d] ? d : -1, Rc);
+        } else {
+            load_face(P, b.UR, nt, gl, rl[d] ? d : -1, L);
+            load_face(P, b.UL, nt, gr, rr[d] ? d : -1, Rc);
+        }
         FluxV<R> F;
         R Ss, vstar[3] = {R(0.0), R(0.0), R(0.0)};
         int side = face_flux(P, L, Rc, d, F, Ss, vstar, b.scal);
