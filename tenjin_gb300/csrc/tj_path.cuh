@@ -64,6 +64,25 @@ __device__ __forceinline__ int find_dom(const DevDomain* doms, int ndom, long lo
     return lo;
 }
 
+// (i, j, k) of entry l of an n0 x n1 x n2 block (i fastest). One domain's
+// cells and faces number below 2^32 at any size that fits the device, so the
+// division runs in 32-bit unsigned arithmetic (a 64-bit division is a long
+// software sequence); the 64-bit form remains for larger blocks.
+__device__ __forceinline__ void split3(long long l, int n0, int n1, int& i, int& j, int& k)
+{
+    if ((unsigned long long)l < 4294967296ULL) {
+        const unsigned u = (unsigned)l, q = u / (unsigned)n0;
+        i = (int)(u - q * (unsigned)n0);
+        const unsigned k2 = q / (unsigned)n1;
+        j = (int)(q - k2 * (unsigned)n1);
+        k = (int)k2;
+    } else {
+        i = (int)(l % n0);
+        j = (int)((l / n0) % n1);
+        k = (int)(l / ((long long)n0 * n1));
+    }
+}
+
 __device__ __forceinline__ int find_dom_face(const DevDomain* doms, int ndom, int d, long long f)
 {
     int lo = 0, hi = ndom - 1;
@@ -146,6 +165,38 @@ __device__ inline void load_state(const PT& P, const R* X, long long nt, long lo
         c.lam = X[P.S_LAM * nt + g];
         c.arl = X[P.S_ARL * nt + g];
     }
+}
+
+// The fields of a carried cell that reconstruction reads (load_state without
+// the conservative variables, which primitiveToConservative recomputes on
+// each face state): the primitives with the reflect_odd sign, the cell's own
+// HJ2 (SOLID) and alphaRhoEps (PLASTIC), and lambda (mixtures).
+template <typename PT, typename R = typename PT::real>
+__device__ inline void load_prims(const PT& P, const R* X, long long nt, long long g, const int* refl, CellT<R>& c)
+{
+    for (int m = 0; m < P.M; ++m) {
+        c.alpha[m] = X[(P.S_ALPHA + m) * nt + g];
+        c.rhok[m] = X[(P.S_RHOK + m) * nt + g];
+    }
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        R u = X[(P.S_VEL + r) * nt + g];
+        if (refl && refl[r]) u = -u;
+        c.vel[r] = u;
+    }
+    c.p = X[P.S_P * nt + g];
+    c.hj2 = R(0.0);
+    if (P.solid) {
+#pragma unroll
+        for (int q = 0; q < 9; ++q) c.V[q] = X[(P.S_V + q) * nt + g];
+        c.hj2 = X[P.S_HJ2 * nt + g];
+    }
+    if (P.plastic)
+        for (int m = 0; m < P.M; ++m) {
+            c.eps[m] = X[(P.S_EPS + m) * nt + g];
+            c.are[m] = X[(P.S_ARE + m) * nt + g];
+        }
+    if (P.nmix) c.lam = X[P.S_LAM * nt + g];
 }
 
 template <typename PT, typename R = typename PT::real>
@@ -423,16 +474,17 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1)
         const int q = find_dom(b.doms, b.ndom, g);
         const DevDomain D = b.doms[q];
         long long l = g - D.off;
-        int i = (int)(l % D.n[0]), j = (int)((l / D.n[0]) % D.n[1]), k = (int)(l / ((long long)D.n[0] * D.n[1]));
+        int i, j, k;
+        split3(l, D.n[0], D.n[1], i, j, k);
         int o[3] = {0, 0, 0};
         o[d] = 1;
         int rm[3], rp[3];
         long long gm = map_cell(P, D, i - o[0], j - o[1], k - o[2], rm);
         long long gp = map_cell(P, D, i + o[0], j + o[1], k + o[2], rp);
         CellT<R> um, u0, up, L, Rc;
-        load_state(P, X, nt, gm, rm, um);
-        load_state(P, X, nt, g, nullptr, u0);
-        load_state(P, X, nt, gp, rp, up);
+        load_prims(P, X, nt, gm, rm, um);
+        load_prims(P, X, nt, g, nullptr, u0);
+        load_prims(P, X, nt, gp, rp, up);
         L = u0;
         Rc = u0;
         if (P.muscl) {  // MUSCLextrapolate over the primitive list
@@ -829,7 +881,8 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1) k_flux(PT P, Path
         int nfv[3] = {D.n[0], D.n[1], D.n[2]};
         nfv[d] += 1;
         long long l = f - D.foff[d];
-        int i = (int)(l % nfv[0]), j = (int)((l / nfv[0]) % nfv[1]), k = (int)(l / ((long long)nfv[0] * nfv[1]));
+        int i, j, k;
+        split3(l, nfv[0], nfv[1], i, j, k);
         int o[3] = {0, 0, 0};
         o[d] = 1;
         int rl[3], rr[3];
@@ -1102,7 +1155,8 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1)
         const int q = find_dom(b.doms, b.ndom, g);
         const DevDomain D = b.doms[q];
         long long l = g - D.off;
-        int i = (int)(l % D.n[0]), j = (int)((l / D.n[0]) % D.n[1]), k = (int)(l / ((long long)D.n[0] * D.n[1]));
+        int i, j, k;
+        split3(l, D.n[0], D.n[1], i, j, k);
         int o[3] = {0, 0, 0};
         o[d] = 1;
         const long long f0 = face_index(D, d, i, j, k), f1 = face_index(D, d, i + o[0], j + o[1], k + o[2]);
