@@ -240,6 +240,28 @@ int tj_forward(tj_ctx* ctx, int domain, const double* prim0, const double* eos, 
                int stride);
 int tj_backward(tj_ctx* ctx, int domain, const double* grad_state, double* grad_prim0, double* grad_eos);
 
+/* Tangent-linear (forward-mode) run of the update: one directional
+ * derivative of the final state. The reference has no derivative; the run is
+ * the FP64 path (its per-direction kernels instantiated with values that
+ * carry a direction) from the initial state of the primitives prim0 (the
+ * tj_set_primitive layout, without mixture words) along dprim0 (same layout,
+ * NULL: zero) and the EOS parameters along deos (HOST,
+ * [n_materials][TJ_MAX_EOS_PARAMS], NULL: zero; eos as in tj_forward), over
+ * nsteps steps of advance with the post-advance operators (main.cpp:145-187)
+ * with dt[n] (HOST). Every configuration of a TJ_PRECISION_FP64 context with
+ * one domain and no mixtures: fluids and solids, the 5-wave solver, the
+ * plastic radial return, cleanUpV, the radial source, BVD-THINC. Branches
+ * are differentiated at the side the FP64 run takes, whose values the run
+ * reproduces bit for bit. state (may be NULL) receives the final values and
+ * dstate their directions, in the tj_download_domain layout (components
+ * derived from the carried ones -- sound speed, USTAR, sigma, VSTAR, devH --
+ * are zero); prim0, dprim0, state and dstate may be host or device pointers.
+ * The context's own state is not changed. With tj_forward / tj_backward on
+ * the same run, <grad_state, dstate> = <grad_prim0, dprim0> + <grad_eos,
+ * deos> to rounding. */
+int tj_tangent(tj_ctx* ctx, int domain, const double* prim0, const double* dprim0, const double* eos,
+               const double* deos, int nsteps, const double* dt, double* state, double* dstate);
+
 /* Time step without any device allocation. No counterpart in the reference:
  * it exists for callers that cannot allocate device memory themselves (a
  * host whose framework owns the GPU's memory pool, a plugin restricted to the

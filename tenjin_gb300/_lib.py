@@ -87,6 +87,8 @@ SIGNATURES = [
     ("tj_kernel_config", _I, [_P, ctypes.c_char_p, ctypes.c_ulong]),
     ("tj_forward", _I, [_P, _I, ctypes.c_void_p, _PD, _I, _PD, _I]),
     ("tj_backward", _I, [_P, _I, ctypes.c_void_p, ctypes.c_void_p, _PD]),
+    ("tj_tangent", _I, [_P, _I, ctypes.c_void_p, ctypes.c_void_p, _PD, _PD, _I, _PD, ctypes.c_void_p,
+                        ctypes.c_void_p]),
 ]
 
 _lib = None

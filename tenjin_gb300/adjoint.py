@@ -98,6 +98,27 @@ class AdjointRun:
                                                ge.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
         return grad_prim, ge
 
+    def tangent(self, prim0: torch.Tensor, dprim0: Optional[torch.Tensor], eos: np.ndarray,
+                deos: Optional[np.ndarray], dts: np.ndarray, want_state: bool = False):
+        """The directional derivative of the final state (tj_tangent) along
+        dprim0 (same layout as prim0, None: zero) and deos ((M,
+        TJ_MAX_EOS_PARAMS), None: zero), from the same FP64 update as
+        forward(). Returns (state or None, dstate) on prim0's device."""
+        prim0 = prim0.detach().contiguous().to(torch.float64)
+        dp = None if dprim0 is None else dprim0.detach().contiguous().to(torch.float64)
+        eos = np.ascontiguousarray(eos, dtype=np.float64)
+        de = None if deos is None else np.ascontiguousarray(deos, dtype=np.float64)
+        dts = np.ascontiguousarray(dts, dtype=np.float64)
+        if prim0.is_cuda:
+            torch.cuda.current_stream().synchronize()
+        st = torch.empty(self.shape_state, dtype=torch.float64, device=prim0.device) if want_state else None
+        ds = torch.empty(self.shape_state, dtype=torch.float64, device=prim0.device)
+        dptr = lambda a: None if a is None else a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        self.sim._check(self.sim.L.tj_tangent(self.sim.h, 0, _ptr(prim0), None if dp is None else _ptr(dp),
+                                              dptr(eos), dptr(de), len(dts), dptr(dts),
+                                              None if st is None else _ptr(st), _ptr(ds)))
+        return st, ds
+
     def close(self):
         self.sim.close()
 

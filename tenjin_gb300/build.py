@@ -34,6 +34,8 @@ UNITS = {
     "tj_noalloc.cu": ["-fmad=false"],
     # the adjoint's forward average must match the FP64 path bit for bit
     "tj_adjoint.cu": ["-fmad=false"],
+    # tangent-linear runs: values bit for bit those of the FP64 path
+    "tj_tangent.cu": ["-fmad=false"],
 }
 
 # The per-direction kernels, one object per (type, material count, direction)
@@ -45,6 +47,13 @@ INSTANCES = {
                              "-fmad=false" if r == 64 else "-use_fast_math"])
     for r in (64, 32) for m, d in _INST
 }
+# the tangent instance (tj_dual.cuh): two materials along x and y, and the
+# generic instance for every other material count and direction
+INSTANCES.update({
+    f"tj_path_t_m{m}_d{'g' if d < 0 else d}.o":
+        ("tj_path_inst.cu", ["-DTJ_INST_R=128", f"-DTJ_INST_M={m}", f"-DTJ_INST_D={d}", "-fmad=false"])
+    for m, d in [(2, 0), (2, 1), (0, -1)]
+})
 
 
 def nvcc() -> str:

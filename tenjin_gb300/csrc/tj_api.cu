@@ -12,6 +12,7 @@
 
 #include "tj_fp64.cuh"
 #include "tj_adjoint.cuh"
+#include "tj_tangent.cuh"
 #include "tj_mixed.cuh"
 #include "tj_layout.h"
 #include "tj_types.h"
@@ -133,6 +134,7 @@ struct tj_ctx {
     EventProf* prof = nullptr;
     long long graph_launches = 0;
     AdjState* adj = nullptr;  // checkpoints and buffers of tj_forward / tj_backward
+    TanState* tan = nullptr;  // buffers of tj_tangent
     double* cons = nullptr;   // conservation sums: partials, then the M + 4 results
 };
 
@@ -195,6 +197,8 @@ void free_dev(tj_ctx* c)
     mixed_free(c->mixed);
     if (c->graph_exec) { cudaGraphExecDestroy(c->graph_exec); c->graph_exec = nullptr; }
     adj_destroy(c->adj);
+    tan_destroy(c->tan);
+    c->tan = nullptr;
     c->adj = nullptr;
 }
 
@@ -1092,6 +1096,50 @@ int tj_backward(tj_ctx* c, int q, const double* grad_state, double* grad_prim0, 
     TJ_CUDA(c, cudaStreamSynchronize(c->stream));
     TJ_CUDA(c, cudaGetLastError());
     return check_status(c);
+}
+
+int tj_tangent(tj_ctx* c, int q, const double* prim0, const double* dprim0, const double* eos, const double* deos,
+               int nsteps, const double* dt, double* state, double* dstate)
+{
+    if (!c || !prim0 || !dt || !dstate || nsteps < 1) return fail(c, TJ_ERR_ARG, "bad tj_tangent arguments");
+    int e = need_state(c);
+    if (e) return e;
+    if (q != 0 || c->doms.size() != 1) return fail(c, TJ_ERR_ARG, "tj_tangent: one domain");
+    if (c->params.precision != TJ_PRECISION_FP64) return fail(c, TJ_ERR_ARG, "tj_tangent runs the FP64 path");
+    if (c->P.nmix) return fail(c, TJ_ERR_ARG, "tj_tangent: no mixtures (the mixture EOS root find)");
+    for (int n = 0; n < nsteps; ++n)
+        if (!(dt[n] > 0.0)) return fail(c, TJ_ERR_ARG, "tj_tangent: dt must be positive");
+    if (eos)
+        for (int m = 0; m < c->P.M; ++m)
+            for (int k = 0; k < c->params.materials[m].nparams && k < TJ_MAX_EOS_PARAMS; ++k) {
+                c->P.prm[m][k] = eos[m * TJ_MAX_EOS_PARAMS + k];
+                c->params.materials[m].params[k] = eos[m * TJ_MAX_EOS_PARAMS + k];
+            }
+    const size_t N = (size_t)c->ntot;
+    const size_t nprim = 2 * c->P.M + 4 + (c->P.solid ? 9 : 0) + (c->P.plastic ? c->P.M : 0);
+    const size_t pw = nprim * N, aw = (size_t)c->P.NCOMP * N;
+    e = ensure_staging(c, sizeof(double) * (2 * pw + 2 * aw));
+    if (e) return e;
+    double* dprim = c->staging;
+    double* dd = dprim + pw;
+    double* ap = dd + pw;
+    double* dap = ap + aw;
+    TJ_CUDA(c, cudaMemcpyAsync(dprim, prim0, sizeof(double) * pw, cudaMemcpyDefault, c->stream));
+    if (dprim0) TJ_CUDA(c, cudaMemcpyAsync(dd, dprim0, sizeof(double) * pw, cudaMemcpyDefault, c->stream));
+    if (!c->tan) c->tan = tan_create();
+    Fp64Bufs b = bufs(c);
+    long long n = tan_run(c->tan, c->P, b, 0, dprim, dprim0 ? dd : nullptr, deos, nsteps, dt, state ? ap : nullptr,
+                          dap, c->stream);
+    if (n < 0) return fail(c, (int)n, "tj_tangent: device allocation failed");
+    c->launches += n;
+    if (state) TJ_CUDA(c, cudaMemcpyAsync(state, ap, sizeof(double) * aw, cudaMemcpyDefault, c->stream));
+    TJ_CUDA(c, cudaMemcpyAsync(dstate, dap, sizeof(double) * aw, cudaMemcpyDefault, c->stream));
+    int status = 0;
+    e = tan_status(c->tan, &status, c->stream);
+    if (e) return fail(c, e, "tj_tangent: status read failed");
+    TJ_CUDA(c, cudaGetLastError());
+    if (status) return fail(c, status, "tj_tangent: a kernel reported an error");
+    return TJ_OK;
 }
 
 int tj_kernel_config(const tj_ctx* c, char* buf, unsigned long len)

@@ -8,6 +8,8 @@
 // which is x itself in binary64.
 #pragma once
 
+#include <type_traits>
+
 #include <cstdint>
 
 #include "tj_math.cuh"
@@ -18,6 +20,13 @@ namespace tj {
 // ---------------------------------------------------------------------------
 // Per-cell state in registers (the reference's Cell view, cell.h:42-84).
 // ---------------------------------------------------------------------------
+// Equality of bit patterns (the repeated cleanUpAlpha's convergence test).
+__device__ __forceinline__ bool same_bits(double a, double b)
+{
+    return __double_as_longlong(a) == __double_as_longlong(b);
+}
+__device__ __forceinline__ bool same_bits(float a, float b) { return __float_as_int(a) == __float_as_int(b); }
+
 template <typename R>
 struct CellT {
     R alpha[TJ_MAX_MAT], arho[TJ_MAX_MAT], rhok[TJ_MAX_MAT];
@@ -688,7 +697,8 @@ __device__ __forceinline__ int c2p(const PT& P, CellT<typename PT::real>& c)
     } else {
         if (P.nmix) {  // :104-113
             c.lam = c.arl / c.arho[0];
-            err = mix_root_find(P, c, ke);
+            // binary64 only: the tangent instance takes no mixtures
+            if constexpr (std::is_same<R, double>::value) err = mix_root_find(P, c, ke);
         }
         c.p = (c.E - ke - eff_e_nonthermal(P, c) + eff_p_nonthermal(P, c)) / (eff_invG(P, c));
     }

@@ -592,7 +592,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1)
                 if (e) set_status(b.scal, e);
                 bool same = true;
                 for (int m = 0; m < P.M; ++m)
-                    same &= (__double_as_longlong(before[m]) == __double_as_longlong(S.alpha[m]));
+                    same &= same_bits(before[m], S.alpha[m]);
                 if (same) break;
             }
         }

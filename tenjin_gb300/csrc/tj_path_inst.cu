@@ -1,10 +1,17 @@
 // One instance of the per-direction launchers (tj_path_launch.cuh), selected
 // at compile time: TJ_INST_R = 64 (binary64, DevParams) or 32 (binary32,
 // DevParams32); TJ_INST_M = material count, 0 for the generic instance;
-// TJ_INST_D = direction, -1 for the generic instance. The CFL pass is
-// instantiated with the first direction of each material count.
+// TJ_INST_D = direction, -1 for the generic instance; TJ_INST_R = 128 is the
+// tangent instance (DevParamsT, tj_dual.cuh), which has no CFL pass. The CFL
+// pass is instantiated with the first direction of each material count.
+#if defined(TJ_INST_R) && TJ_INST_R == 128
+#include "tj_dual.cuh"
+#endif
 #include "tj_path.cuh"
 #include "tj_path_launch.cuh"
+#if defined(TJ_INST_R) && TJ_INST_R == 128
+#include "tj_dual_path.cuh"
+#endif
 
 #if !defined(TJ_INST_R) || !defined(TJ_INST_M) || !defined(TJ_INST_D)
 #error "TJ_INST_R, TJ_INST_M and TJ_INST_D select the instance"
@@ -55,6 +62,8 @@ int path_cfl(const PT& P, const PathBufs<typename PT::real>& b, const typename P
 
 #if TJ_INST_R == 64
 using InstBase = DevParams;
+#elif TJ_INST_R == 128
+using InstBase = DevParamsT;
 #else
 using InstBase = DevParams32;
 #endif
@@ -66,7 +75,7 @@ using InstPT = InstBase;
 
 template int path_dir<InstPT, TJ_INST_D>(const InstPT&, const PathBufs<InstPT::real>&, const InstPT::real*,
                                          InstPT::real*, int, int, int, int, cudaStream_t, Prof*);
-#if TJ_INST_D <= 0
+#if TJ_INST_D <= 0 && TJ_INST_R != 128
 template int path_cfl<InstPT>(const InstPT&, const PathBufs<InstPT::real>&, const InstPT::real*, cudaStream_t, Prof*);
 #endif
 
