@@ -266,12 +266,14 @@ def run_gpu_arm(args):
     if precision == MIXED and args.fp64_compare:
         accuracy = accuracy_runs(case, args.accuracy_steps)
     # the second half of the metric: adjoint / forward time on the 2-D
-    # interface problem at 512^2, 200 steps, with a finite-difference check
+    # interface problem at 512^2, 200 steps, checked against the tangent-linear
+    # run (and, on request, against central differences)
     configs = other_configs() if args.other_configs and rank == 0 else None
     adjoint = None
     if args.adjoint_dirs >= 0 and rank == 0:
         from tenjin_gb300.adjoint import interface_problem_check
-        adjoint = interface_problem_check(512, 200, 20, args.adjoint_dirs)
+        adjoint = interface_problem_check(512, 200, 20, args.adjoint_dirs, background=args.adjoint_background,
+                                          tlm_dirs=args.adjoint_tlm_dirs)
     g.close()
     value = ncell * args.steps * ws / (ms / 1e3)
     line = {
@@ -496,8 +498,12 @@ def main():
     ap.add_argument("--accuracy-steps", type=int, default=2000, help="steps of the precision comparison")
     ap.add_argument("--no-other-configs", dest="other_configs", action="store_false",
                     help="skip the 3-D configurations")
-    ap.add_argument("--adjoint-dirs", type=int, default=16,
+    ap.add_argument("--adjoint-dirs", type=int, default=0,
                     help="finite-difference directions of the adjoint check (-1: skip the adjoint)")
+    ap.add_argument("--adjoint-tlm-dirs", type=int, default=64,
+                    help="directions of the adjoint checked against the tangent-linear run")
+    ap.add_argument("--adjoint-background", type=float, default=0.0,
+                    help="smooth background of the adjoint problem's base state (0: the problem as stated)")
     ap.add_argument("--no-fp64-compare", dest="fp64_compare", action="store_false")
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)

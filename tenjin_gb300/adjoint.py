@@ -160,7 +160,7 @@ def density_misfit(state: torch.Tensor, target: torch.Tensor, M: int, cell_area:
 
 def interface_problem_check(n: int = 512, nsteps: int = 200, stride: int = 20, ndir: int = 64,
                             step_rho: float = 1e-8, step_eos: float = 1e-8, seed: int = 0,
-                            background: float = 1e-3) -> dict:
+                            background: float = 1e-3, tlm_dirs: int = 0) -> dict:
     """The adjoint on the 2-D water/air interface problem: n^2 cells, nsteps
     steps with the dt schedule of a plain FP64 run, checkpoints every
     `stride` steps, J = 1/2 sum (rho - rho_target)^2 dx^2 with rho_target =
@@ -177,7 +177,13 @@ def interface_problem_check(n: int = 512, nsteps: int = 200, stride: int = 20, n
     discrete choices (limiter, BVD-THINC, wave-speed maxima, HLLC side) of
     cells whose margin is below the step, an error that falls with the step:
     at 128^2 and 60 steps the EOS part goes from 4e-5 at 1e-6 to 3e-6 at 1e-8
-    while rounding stays below 1e-6."""
+    while rounding stays below 1e-6.
+
+    `tlm_dirs` further directions (the same kind) are checked against the
+    tangent-linear run (tj_tangent): <grad_state, dstate> against
+    <grad_prim0, dprim0> + <grad_eos, deos>. Both differentiate the branches
+    the FP64 run takes, so they agree to rounding with or without the
+    background, where central differences cannot."""
     import time
 
     from . import cases
@@ -214,13 +220,36 @@ def interface_problem_check(n: int = 512, nsteps: int = 200, stride: int = 20, n
     def central(v, ve, h):
         return (J(prim0 + h * v, eos + h * ve) - J(prim0 - h * v, eos - h * ve)) / (2 * h)
 
-    errs, errs_rho, errs_eos = [], [], []
-    for _ in range(ndir):
+    def direction(r):
         v = np.zeros_like(prim0)
         for m in range(M):
-            v[M + m, 0] = cases.smooth_field(rng, n) * prim0[M + m, 0]
+            v[M + m, 0] = cases.smooth_field(r, n) * prim0[M + m, 0]
         ve = np.zeros_like(eos)
-        ve[:, 0:2] = rng.standard_normal((M, 2)) * eos[:, 0:2]
+        ve[:, 0:2] = r.standard_normal((M, 2)) * eos[:, 0:2]
+        return v, ve
+
+    tlm = None
+    if tlm_dirs > 0:
+        gsn = gs.cpu().numpy()
+        terrs = []
+        ts = []
+        rng_t = np.random.default_rng(seed + 1000)
+        for _ in range(tlm_dirs):
+            v, ve = direction(rng_t)
+            torch.cuda.synchronize()
+            t3 = time.perf_counter()
+            _, ds = run.tangent(prim, torch.from_numpy(v).cuda(), eos, ve, dts)
+            ts.append(time.perf_counter() - t3)
+            tl = float((gsn * ds.cpu().numpy()).sum())
+            ad = float((gp * v).sum() + (ge * ve).sum())
+            terrs.append(abs(tl - ad) / max(abs(tl), abs(ad)))
+        e = np.array(terrs)
+        tlm = {"directions": tlm_dirs, "max_rel_err": float(e.max()), "median_rel_err": float(np.median(e)),
+               "frac_within_1e-9": float((e <= 1e-9).mean()), "tangent_run_s": float(np.median(ts))}
+
+    errs, errs_rho, errs_eos = [], [], []
+    for _ in range(ndir):
+        v, ve = direction(rng)
         fd_r, ad_r = central(v, np.zeros_like(eos), step_rho), float((gp * v).sum())
         fd_e, ad_e = central(np.zeros_like(prim0), ve, step_eos), float((ge * ve).sum())
         errs_rho.append(abs(fd_r - ad_r) / max(abs(fd_r), abs(ad_r)))
@@ -237,10 +266,10 @@ def interface_problem_check(n: int = 512, nsteps: int = 200, stride: int = 20, n
                 "frac_within_1e-5": float((e <= 1e-5).mean())}
 
     fd = {"directions": ndir, "step_rho": step_rho, "step_eos": step_eos, "combined": summary(errs),
-          "rho_part": summary(errs_rho), "eos_part": summary(errs_eos)}
+          "rho_part": summary(errs_rho), "eos_part": summary(errs_eos)} if ndir > 0 else None
     return {"workload": f"2-D water/air interface, {n}x{n}, {nsteps} steps, THINC, checkpoint every {stride}",
             "forward_s": fwd_s, "backward_s": bwd_s, "ratio": bwd_s / fwd_s,
-            "forward_cell_updates_per_s": n * n * nsteps / fwd_s, "fd_check": fd,
+            "forward_cell_updates_per_s": n * n * nsteps / fwd_s, "fd_check": fd, "tangent_check": tlm,
             "inputs": "initial rho_k fields (smooth seeded directions) and gamma, p_ref of both materials",
             "base_background": background}
 
@@ -256,6 +285,7 @@ if __name__ == "__main__":
     ap.add_argument("--dirs", type=int, default=64)
     ap.add_argument("--step-rho", type=float, default=1e-8, help="relative step along the partial densities")
     ap.add_argument("--step-eos", type=float, default=1e-8, help="relative step along (gamma, p_ref)")
+    ap.add_argument("--tlm-dirs", type=int, default=0, help="directions checked against the tangent-linear run")
     ap.add_argument("--background", type=float, default=1e-3,
                     help="relative amplitude of the smooth background of the base state (0: the configuration as "
                          "stated, with exactly uniform regions)")
@@ -263,4 +293,4 @@ if __name__ == "__main__":
     from . import build
     build.build()
     print(json.dumps(interface_problem_check(a.n, a.steps, a.stride, a.dirs, step_rho=a.step_rho,
-                                             step_eos=a.step_eos, background=a.background)))
+                                             step_eos=a.step_eos, background=a.background, tlm_dirs=a.tlm_dirs)))
