@@ -219,23 +219,31 @@ int tj_kernel_config(const tj_ctx* ctx, char* buf, unsigned long len);
 
 /* Adjoint pair (the forward / backward of a torch.autograd.Function). The
  * reference has no adjoint; the pair differentiates its per-timestep update
- * (main.cpp:145-170 with the loop of main.cpp:121-191) for 2-D fluids with
- * the stiffened-gas EOS, one domain, TJ_PRECISION_FP64, dt frozen.
+ * (main.cpp:145-187 with the loop of main.cpp:121-191), TJ_PRECISION_FP64,
+ * one domain, dt frozen. 2-D fluids with the stiffened-gas EOS (BVD-THINC
+ * included) take the dedicated reverse sweep; every other configuration
+ * without BVD-THINC and mixtures (1-, 2- and 3-D, solids with the 5-wave
+ * solver, the plastic radial return, cleanUpV, the radial source, every EOS)
+ * takes the general reverse mode, built from local Jacobians of the FP64
+ * path's own device functions (forward-mode passes, one per input of each
+ * cell's update and each face's Riemann problem): exact, deterministic, a
+ * backward 50-110 times the forward's time.
  * tj_forward: initial state from the primitives prim0 (the tj_set_primitive
- * layout) with the EOS parameters eos ([n_materials][TJ_MAX_EOS_PARAMS] in
- * the getMaterialParameters order, initialise.cpp:125-235; NULL keeps the
- * current ones), THINC scratch zeroed, then nsteps steps of advance +
- * cleanUpAlpha with dt[n] (HOST array); the state and the THINC scratch are
- * saved every `stride` steps. The final state is the context's state.
+ * layout without mixture words) with the EOS parameters eos
+ * ([n_materials][TJ_MAX_EOS_PARAMS] in the getMaterialParameters order,
+ * initialise.cpp:125-235; NULL keeps the current ones), THINC scratch zeroed,
+ * then nsteps steps of advance and the post-advance operators with dt[n]
+ * (HOST array); the state (and the THINC scratch) are saved every `stride`
+ * steps. The final state is the context's state.
  * tj_backward: from grad_state, the gradient of a scalar objective with
  * respect to the final state (tj_download_domain layout; components derived
- * from others - sound speed, sigma, USTAR - are ignored), to the gradient with
- * respect to prim0 (grad_prim0, same layout as prim0) and to the EOS
- * parameters (grad_eos, HOST, [n_materials][TJ_MAX_EOS_PARAMS]; nonzero for
- * params 0-2). Each interval of `stride` steps is recomputed from its
- * checkpoint and reversed; limiter, THINC and Riemann-solver branches are
- * differentiated at their forward choice. prim0, grad_state and grad_prim0
- * may be host or device pointers. */
+ * from others - sound speed, sigma, USTAR, VSTAR, devH - are ignored), to the
+ * gradient with respect to prim0 (grad_prim0, same layout as prim0) and to
+ * the EOS parameters (grad_eos, HOST, [n_materials][TJ_MAX_EOS_PARAMS]). Each
+ * interval of `stride` steps is recomputed from its checkpoint and reversed;
+ * limiter, THINC, Riemann-solver and yield branches are differentiated at
+ * their forward choice. prim0, grad_state and grad_prim0 may be host or
+ * device pointers. */
 int tj_forward(tj_ctx* ctx, int domain, const double* prim0, const double* eos, int nsteps, const double* dt,
                int stride);
 int tj_backward(tj_ctx* ctx, int domain, const double* grad_state, double* grad_prim0, double* grad_eos);

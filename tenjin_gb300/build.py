@@ -36,6 +36,8 @@ UNITS = {
     "tj_adjoint.cu": ["-fmad=false"],
     # tangent-linear runs: values bit for bit those of the FP64 path
     "tj_tangent.cu": ["-fmad=false"],
+    # the general reverse mode differentiates the FP64 path's own arithmetic
+    "tj_adjoint_gen.cu": ["-fmad=false"],
 }
 
 # The per-direction kernels, one object per (type, material count, direction)

@@ -13,6 +13,7 @@
 #include "tj_fp64.cuh"
 #include "tj_adjoint.cuh"
 #include "tj_tangent.cuh"
+#include "tj_adjoint_gen.cuh"
 #include "tj_mixed.cuh"
 #include "tj_layout.h"
 #include "tj_types.h"
@@ -135,6 +136,8 @@ struct tj_ctx {
     long long graph_launches = 0;
     AdjState* adj = nullptr;  // checkpoints and buffers of tj_forward / tj_backward
     TanState* tan = nullptr;  // buffers of tj_tangent
+    GenAdj* gen = nullptr;    // the general reverse mode (configurations the 2-D adjoint does not cover)
+    bool adj_general = false; // the last tj_forward took the general reverse mode
     double* cons = nullptr;   // conservation sums: partials, then the M + 4 results
 };
 
@@ -199,6 +202,8 @@ void free_dev(tj_ctx* c)
     adj_destroy(c->adj);
     tan_destroy(c->tan);
     c->tan = nullptr;
+    gen_destroy(c->gen);
+    c->gen = nullptr;
     c->adj = nullptr;
 }
 
@@ -1032,8 +1037,12 @@ int tj_forward(tj_ctx* c, int q, const double* prim0, const double* eos, int nst
     if (e) return e;
     if (q != 0) return fail(c, TJ_ERR_ARG, "tj_forward: domain 0 only");
     if (c->params.precision != TJ_PRECISION_FP64) return fail(c, TJ_ERR_ARG, "tj_forward runs the FP64 path");
-    const char* why = adj_unsupported(c->P, (int)c->doms.size());
-    if (why) return fail(c, TJ_ERR_ARG, why);
+    // the 2-D fluid adjoint where it applies, the general reverse mode else
+    const bool general = adj_unsupported(c->P, (int)c->doms.size()) != nullptr;
+    if (general) {
+        const char* why = gen_unsupported(c->P, (int)c->doms.size());
+        if (why) return fail(c, TJ_ERR_ARG, why);
+    }
     for (int n = 0; n < nsteps; ++n)
         if (!(dt[n] > 0.0)) return fail(c, TJ_ERR_ARG, "tj_forward: dt must be positive");
     if (eos)
@@ -1043,7 +1052,7 @@ int tj_forward(tj_ctx* c, int q, const double* prim0, const double* eos, int nst
                 c->params.materials[m].params[k] = eos[m * TJ_MAX_EOS_PARAMS + k];
             }
     const DevDomain& D = c->doms[0];
-    const size_t nprim = 2 * c->P.M + 4;
+    const size_t nprim = 2 * c->P.M + 4 + (c->P.solid ? 9 : 0) + (c->P.plastic ? c->P.M : 0);
     const size_t bytes = sizeof(double) * nprim * (size_t)c->ntot;
     e = ensure_staging(c, bytes);
     if (e) return e;
@@ -1058,8 +1067,15 @@ int tj_forward(tj_ctx* c, int q, const double* prim0, const double* eos, int nst
     }
     Fp64Bufs b = bufs(c);
     c->launches += fp64_prim_to_state(c->P, b, 0, c->staging, c->A, c->stream);
-    if (!c->adj) c->adj = adj_create();
-    long long n = adj_forward(c->adj, c->P, b, D, dt, nsteps, stride, c->stream);
+    c->adj_general = general;
+    long long n;
+    if (general) {
+        if (!c->gen) c->gen = gen_create();
+        n = gen_forward(c->gen, c->P, b, c->staging, (int)nprim, dt, nsteps, stride, c->stream);
+    } else {
+        if (!c->adj) c->adj = adj_create();
+        n = adj_forward(c->adj, c->P, b, D, dt, nsteps, stride, c->stream);
+    }
     if (n < 0) return fail(c, (int)n, "tj_forward: device allocation failed");
     c->launches += n;
     TJ_CUDA(c, cudaGetLastError());
@@ -1076,6 +1092,27 @@ int tj_backward(tj_ctx* c, int q, const double* grad_state, double* grad_prim0, 
     int e = need_state(c);
     if (e) return e;
     if (q != 0) return fail(c, TJ_ERR_ARG, "tj_backward: domain 0 only");
+    if (c->adj_general) {
+        if (!c->gen) return fail(c, TJ_ERR_STATE, "tj_backward needs a tj_forward first");
+        const long long N = c->ntot;
+        const size_t nprim = 2 * c->P.M + 4 + (c->P.solid ? 9 : 0) + (c->P.plastic ? c->P.M : 0);
+        const size_t in_w = (size_t)c->P.NCOMP * N, out_w = nprim * (size_t)N;
+        e = ensure_staging(c, sizeof(double) * (in_w + out_w));
+        if (e) return e;
+        double* gin = c->staging;
+        double* gout = c->staging + in_w;
+        TJ_CUDA(c, cudaMemcpyAsync(gin, grad_state, sizeof(double) * in_w, cudaMemcpyDefault, c->stream));
+        int np[TJ_MAX_MATERIALS];
+        for (int m = 0; m < c->P.M; ++m) np[m] = c->params.materials[m].nparams;
+        Fp64Bufs b = bufs(c);
+        long long n = gen_backward(c->gen, c->P, b, gin, gout, grad_eos, np, c->stream);
+        if (n < 0) return fail(c, (int)n, "tj_backward: no forward to reverse");
+        c->launches += n;
+        TJ_CUDA(c, cudaMemcpyAsync(grad_prim0, gout, sizeof(double) * out_w, cudaMemcpyDefault, c->stream));
+        TJ_CUDA(c, cudaStreamSynchronize(c->stream));
+        TJ_CUDA(c, cudaGetLastError());
+        return check_status(c);
+    }
     if (!c->adj) return fail(c, TJ_ERR_STATE, "tj_backward needs a tj_forward first");
     const DevDomain& D = c->doms[0];
     const int nx = D.n[0], ny = D.n[1];

@@ -1142,6 +1142,131 @@ __device__ inline void radial_source(const PT& P, CellT<R>& c, const R* sg, int 
 // Update of one direction; last direction: c2p; second stage: average and
 // the post-advance operators of main.cpp:145-187.
 // ---------------------------------------------------------------------------
+// Flux words of the two faces of a cell in the face arrays (side 0: the
+// face below the cell along d, 1: the face above).
+template <typename R>
+struct FacePairGlobal {
+    const R* FX;
+    long long nf, f0, f1;
+    __device__ __forceinline__ R operator()(int w, int s) const { return FX[(long long)w * nf + (s ? f1 : f0)]; }
+};
+
+// Update of cell g along d from the fluxes of its two faces (FXW(w, side));
+// the last direction: c2p; second stage: the average and the post-advance
+// operators of main.cpp:145-187.
+template <typename PT, typename FA, typename R = typename PT::real>
+__device__ __forceinline__ void update_cell(const PT& P, const PathBufs<R>& b, const R* __restrict__ X, R* Y,
+                                            long long g, const DevDomain& D, int i, int d, int first, int last,
+                                            int finish, R dtdx_num, const FA& FXW)
+{
+    const long long nt = b.ntot;
+    CellT<R> U, Yc;
+    load_state(P, X, nt, g, nullptr, U);
+    if (first) Yc = U;
+    else load_state(P, Y, nt, g, nullptr, Yc);
+    const R dtdx = dtdx_num / (R)D.dx[d];
+    for (int m = 0; m < P.M; ++m) {
+        Yc.alpha[m] += dtdx * (FXW(P.X_ALPHA + m, 0) - FXW(P.X_ALPHA + m, 1) - U.alpha[m] * (FXW(P.X_SSTAR, 0) - FXW(P.X_SSTAR, 1)));
+        Yc.arho[m] += dtdx * (FXW(P.X_ARHO + m, 0) - FXW(P.X_ARHO + m, 1));
+    }
+#pragma unroll
+    for (int r = 0; r < 3; ++r) Yc.rhou[r] += dtdx * (FXW(P.X_RHOU + r, 0) - FXW(P.X_RHOU + r, 1));
+    if constexpr (sizeof(R) == 4) dd_add32(Yc.E, Yc.Elo, dtdx * (FXW(P.X_E, 0) - FXW(P.X_E, 1)));
+    else Yc.E += dtdx * (FXW(P.X_E, 0) - FXW(P.X_E, 1));
+    if (P.solid)
+#pragma unroll
+        for (int qq = 0; qq < 9; ++qq) {
+            int row = qq / 3, col = qq % 3;
+            Yc.V[qq] += dtdx * (FXW(P.X_V + qq, 0) - FXW(P.X_V + qq, 1) -
+                                (R(2.0) / R(3.0)) * U.V[qq] * (FXW(P.X_SSTAR, 0) - FXW(P.X_SSTAR, 1)) +
+                                U.vel[row] * (FXW(P.X_VSTAR + col, 0) - FXW(P.X_VSTAR + col, 1)));
+        }
+    if (P.plastic)
+        for (int m = 0; m < P.M; ++m) Yc.are[m] += dtdx * (FXW(P.X_ARE + m, 0) - FXW(P.X_ARE + m, 1));
+    if (P.nmix) Yc.arl += dtdx * (FXW(P.X_ARL, 0) - FXW(P.X_ARL, 1));
+    if (last) {
+        const int ce = c2p(P, Yc);
+        if (ce) set_status(b.scal, ce);
+        if (finish) {
+            const R p_stage = Yc.p;  // U2's pressure, before the average
+            // U1 = U*0.5 + U2*0.5 over every carried component (hllc.cpp:705)
+            CellT<R> A0;
+            load_state(P, b.A, nt, g, nullptr, A0);
+            for (int m = 0; m < P.M; ++m) {
+                Yc.alpha[m] = (A0.alpha[m] * (R(1.0) / R(2.0))) + (Yc.alpha[m] * (R(1.0) / R(2.0)));
+                Yc.arho[m] = (A0.arho[m] * (R(1.0) / R(2.0))) + (Yc.arho[m] * (R(1.0) / R(2.0)));
+                Yc.rhok[m] = (A0.rhok[m] * (R(1.0) / R(2.0))) + (Yc.rhok[m] * (R(1.0) / R(2.0)));
+                if (P.plastic) {
+                    Yc.eps[m] = (A0.eps[m] * (R(1.0) / R(2.0))) + (Yc.eps[m] * (R(1.0) / R(2.0)));
+                    Yc.are[m] = (A0.are[m] * (R(1.0) / R(2.0))) + (Yc.are[m] * (R(1.0) / R(2.0)));
+                }
+            }
+            Yc.rho = (A0.rho * (R(1.0) / R(2.0))) + (Yc.rho * (R(1.0) / R(2.0)));
+#pragma unroll
+            for (int r = 0; r < 3; ++r) {
+                Yc.rhou[r] = (A0.rhou[r] * (R(1.0) / R(2.0))) + (Yc.rhou[r] * (R(1.0) / R(2.0)));
+                Yc.vel[r] = (A0.vel[r] * (R(1.0) / R(2.0))) + (Yc.vel[r] * (R(1.0) / R(2.0)));
+            }
+            if constexpr (sizeof(R) == 4) avg_pair32(A0.E, A0.Elo, Yc.E, Yc.Elo);
+            else Yc.E = (A0.E * (R(1.0) / R(2.0))) + (Yc.E * (R(1.0) / R(2.0)));
+            Yc.p = (A0.p * (R(1.0) / R(2.0))) + (Yc.p * (R(1.0) / R(2.0)));
+            if (P.solid) {
+#pragma unroll
+                for (int qq = 0; qq < 9; ++qq) Yc.V[qq] = (A0.V[qq] * (R(1.0) / R(2.0))) + (Yc.V[qq] * (R(1.0) / R(2.0)));
+                Yc.hj2 = (A0.hj2 * (R(1.0) / R(2.0))) + (Yc.hj2 * (R(1.0) / R(2.0)));
+            }
+            if (P.nmix) {
+                Yc.rm0 = (A0.rm0 * (R(1.0) / R(2.0))) + (Yc.rm0 * (R(1.0) / R(2.0)));
+                Yc.rm1 = (A0.rm1 * (R(1.0) / R(2.0))) + (Yc.rm1 * (R(1.0) / R(2.0)));
+                Yc.lam = (A0.lam * (R(1.0) / R(2.0))) + (Yc.lam * (R(1.0) / R(2.0)));
+                Yc.arl = (A0.arl * (R(1.0) / R(2.0))) + (Yc.arl * (R(1.0) / R(2.0)));
+            }
+            if (finish == 2) {  // advance() alone: the average only
+                store_state(P, b.A, nt, g, Yc);
+                return;
+            }
+            if (P.reactive && P.nmix) {  // main.cpp:149-152
+                const int re = reactive_cell(P, Yc, dtdx_num);
+                if (re) set_status(b.scal, re);
+            }
+            if (P.plastic) {
+                int e;
+                if constexpr (sizeof(R) == 4) e = plastic_cell_proj64(P, Yc);
+                else e = plastic_cell(P, Yc);
+                c2p(P, Yc);
+                if (e) set_status(b.scal, e);
+            }
+            if (P.radial) {
+                // the stress the reference's U1 holds here: fresh from the
+                // c2p of the plastic or the reactive update, else the
+                // average of U's and U2's (fluids only: -p I each,
+                // boxaccesscellarray.cpp:204-212)
+                const bool fresh = P.plastic || (P.reactive && P.nmix);
+                R sg[9];
+#pragma unroll
+                for (int r = 0; r < 3; ++r)
+#pragma unroll
+                    for (int qq = 0; qq < 3; ++qq) {
+                        const R dl = (R)(r == qq);
+                        sg[3 * r + qq] = fresh ? Yc.sigma[3 * r + qq]
+                                                   : ((-A0.p * dl) * (R(1.0) / R(2.0))) +
+                                                         ((-p_stage * dl) * (R(1.0) / R(2.0)));
+                    }
+                radial_source(P, Yc, sg, i, D.dx[0], dtdx_num);
+                const int rc = c2p(P, Yc);  // geometricSourceTerm (radial.cpp:50)
+                if (rc) set_status(b.scal, rc);
+            }
+            if (P.solid) cleanup_v_cell(P, Yc);
+            int e = cleanup_alpha(P, Yc.alpha);
+            if (e) set_status(b.scal, e);
+            if (b.cell_box[g] == D.nbox - 1 && cell_has_nan(P, Yc)) atomicOr(&b.scal->nan_flag, 1);
+            store_state(P, b.A, nt, g, Yc);
+            return;
+        }
+    }
+    store_state(P, Y, nt, g, Yc);
+}
+
 template <typename PT, int DC = -1, typename R = typename PT::real>
 __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1)
     k_update(PT P, PathBufs<typename PT::real> b, const R* __restrict__ X, R* Y, int dyn_d, int first, int last,
@@ -1159,116 +1284,8 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 2 : 1)
         split3(l, D.n[0], D.n[1], i, j, k);
         int o[3] = {0, 0, 0};
         o[d] = 1;
-        const long long f0 = face_index(D, d, i, j, k), f1 = face_index(D, d, i + o[0], j + o[1], k + o[2]);
-        CellT<R> U, Yc;
-        load_state(P, X, nt, g, nullptr, U);
-        if (first) Yc = U;
-        else load_state(P, Y, nt, g, nullptr, Yc);
-        const R dtdx = dtdx_num / (R)D.dx[d];
-#define FXW(w, f) b.FX[(long long)(w)*nf + (f)]
-        const R dS = FXW(P.X_SSTAR, f0) - FXW(P.X_SSTAR, f1);
-        for (int m = 0; m < P.M; ++m) {
-            Yc.alpha[m] += dtdx * (FXW(P.X_ALPHA + m, f0) - FXW(P.X_ALPHA + m, f1) - U.alpha[m] * (FXW(P.X_SSTAR, f0) - FXW(P.X_SSTAR, f1)));
-            Yc.arho[m] += dtdx * (FXW(P.X_ARHO + m, f0) - FXW(P.X_ARHO + m, f1));
-        }
-        (void)dS;
-#pragma unroll
-        for (int r = 0; r < 3; ++r) Yc.rhou[r] += dtdx * (FXW(P.X_RHOU + r, f0) - FXW(P.X_RHOU + r, f1));
-        if constexpr (sizeof(R) == 4) dd_add32(Yc.E, Yc.Elo, dtdx * (FXW(P.X_E, f0) - FXW(P.X_E, f1)));
-        else Yc.E += dtdx * (FXW(P.X_E, f0) - FXW(P.X_E, f1));
-        if (P.solid)
-#pragma unroll
-            for (int qq = 0; qq < 9; ++qq) {
-                int row = qq / 3, col = qq % 3;
-                Yc.V[qq] += dtdx * (FXW(P.X_V + qq, f0) - FXW(P.X_V + qq, f1) -
-                                    (R(2.0) / R(3.0)) * U.V[qq] * (FXW(P.X_SSTAR, f0) - FXW(P.X_SSTAR, f1)) +
-                                    U.vel[row] * (FXW(P.X_VSTAR + col, f0) - FXW(P.X_VSTAR + col, f1)));
-            }
-        if (P.plastic)
-            for (int m = 0; m < P.M; ++m) Yc.are[m] += dtdx * (FXW(P.X_ARE + m, f0) - FXW(P.X_ARE + m, f1));
-        if (P.nmix) Yc.arl += dtdx * (FXW(P.X_ARL, f0) - FXW(P.X_ARL, f1));
-#undef FXW
-        if (last) {
-            const int ce = c2p(P, Yc);
-            if (ce) set_status(b.scal, ce);
-            if (finish) {
-                const R p_stage = Yc.p;  // U2's pressure, before the average
-                // U1 = U*0.5 + U2*0.5 over every carried component (hllc.cpp:705)
-                CellT<R> A0;
-                load_state(P, b.A, nt, g, nullptr, A0);
-                for (int m = 0; m < P.M; ++m) {
-                    Yc.alpha[m] = (A0.alpha[m] * (R(1.0) / R(2.0))) + (Yc.alpha[m] * (R(1.0) / R(2.0)));
-                    Yc.arho[m] = (A0.arho[m] * (R(1.0) / R(2.0))) + (Yc.arho[m] * (R(1.0) / R(2.0)));
-                    Yc.rhok[m] = (A0.rhok[m] * (R(1.0) / R(2.0))) + (Yc.rhok[m] * (R(1.0) / R(2.0)));
-                    if (P.plastic) {
-                        Yc.eps[m] = (A0.eps[m] * (R(1.0) / R(2.0))) + (Yc.eps[m] * (R(1.0) / R(2.0)));
-                        Yc.are[m] = (A0.are[m] * (R(1.0) / R(2.0))) + (Yc.are[m] * (R(1.0) / R(2.0)));
-                    }
-                }
-                Yc.rho = (A0.rho * (R(1.0) / R(2.0))) + (Yc.rho * (R(1.0) / R(2.0)));
-#pragma unroll
-                for (int r = 0; r < 3; ++r) {
-                    Yc.rhou[r] = (A0.rhou[r] * (R(1.0) / R(2.0))) + (Yc.rhou[r] * (R(1.0) / R(2.0)));
-                    Yc.vel[r] = (A0.vel[r] * (R(1.0) / R(2.0))) + (Yc.vel[r] * (R(1.0) / R(2.0)));
-                }
-                if constexpr (sizeof(R) == 4) avg_pair32(A0.E, A0.Elo, Yc.E, Yc.Elo);
-                else Yc.E = (A0.E * (R(1.0) / R(2.0))) + (Yc.E * (R(1.0) / R(2.0)));
-                Yc.p = (A0.p * (R(1.0) / R(2.0))) + (Yc.p * (R(1.0) / R(2.0)));
-                if (P.solid) {
-#pragma unroll
-                    for (int qq = 0; qq < 9; ++qq) Yc.V[qq] = (A0.V[qq] * (R(1.0) / R(2.0))) + (Yc.V[qq] * (R(1.0) / R(2.0)));
-                    Yc.hj2 = (A0.hj2 * (R(1.0) / R(2.0))) + (Yc.hj2 * (R(1.0) / R(2.0)));
-                }
-                if (P.nmix) {
-                    Yc.rm0 = (A0.rm0 * (R(1.0) / R(2.0))) + (Yc.rm0 * (R(1.0) / R(2.0)));
-                    Yc.rm1 = (A0.rm1 * (R(1.0) / R(2.0))) + (Yc.rm1 * (R(1.0) / R(2.0)));
-                    Yc.lam = (A0.lam * (R(1.0) / R(2.0))) + (Yc.lam * (R(1.0) / R(2.0)));
-                    Yc.arl = (A0.arl * (R(1.0) / R(2.0))) + (Yc.arl * (R(1.0) / R(2.0)));
-                }
-                if (finish == 2) {  // advance() alone: the average only
-                    store_state(P, b.A, nt, g, Yc);
-                    continue;
-                }
-                if (P.reactive && P.nmix) {  // main.cpp:149-152
-                    const int re = reactive_cell(P, Yc, dtdx_num);
-                    if (re) set_status(b.scal, re);
-                }
-                if (P.plastic) {
-                    int e;
-                    if constexpr (sizeof(R) == 4) e = plastic_cell_proj64(P, Yc);
-                    else e = plastic_cell(P, Yc);
-                    c2p(P, Yc);
-                    if (e) set_status(b.scal, e);
-                }
-                if (P.radial) {
-                    // the stress the reference's U1 holds here: fresh from the
-                    // c2p of the plastic or the reactive update, else the
-                    // average of U's and U2's (fluids only: -p I each,
-                    // boxaccesscellarray.cpp:204-212)
-                    const bool fresh = P.plastic || (P.reactive && P.nmix);
-                    R sg[9];
-#pragma unroll
-                    for (int r = 0; r < 3; ++r)
-#pragma unroll
-                        for (int qq = 0; qq < 3; ++qq) {
-                            const R dl = (R)(r == qq);
-                            sg[3 * r + qq] = fresh ? Yc.sigma[3 * r + qq]
-                                                       : ((-A0.p * dl) * (R(1.0) / R(2.0))) +
-                                                             ((-p_stage * dl) * (R(1.0) / R(2.0)));
-                        }
-                    radial_source(P, Yc, sg, i, D.dx[0], dtdx_num);
-                    const int rc = c2p(P, Yc);  // geometricSourceTerm (radial.cpp:50)
-                    if (rc) set_status(b.scal, rc);
-                }
-                if (P.solid) cleanup_v_cell(P, Yc);
-                int e = cleanup_alpha(P, Yc.alpha);
-                if (e) set_status(b.scal, e);
-                if (b.cell_box[g] == D.nbox - 1 && cell_has_nan(P, Yc)) atomicOr(&b.scal->nan_flag, 1);
-                store_state(P, b.A, nt, g, Yc);
-                continue;
-            }
-        }
-        store_state(P, Y, nt, g, Yc);
+        const FacePairGlobal<R> fx{b.FX, nf, face_index(D, d, i, j, k), face_index(D, d, i + o[0], j + o[1], k + o[2])};
+        update_cell(P, b, X, Y, g, D, i, d, first, last, finish, dtdx_num, fx);
     }
 }
 
