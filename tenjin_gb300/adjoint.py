@@ -2,14 +2,18 @@
 ``tj_forward`` / ``tj_backward`` of libtenjin_gpu.so, behind the
 ``torch.autograd.Function`` contract.
 
-The reference has no adjoint. What is differentiated is its update for 2-D
-fluids with the stiffened-gas EOS (advance + cleanUpAlpha, main.cpp:145-170,
-hllc.cpp:579-707) over a time-step schedule frozen from a plain FP64 run at
-the reference parameters (the dt of timestep.cpp:36-70 and main.cpp:128-143).
-Inputs are the initial primitive fields (the layout ``tj_set_primitive``
-takes: alpha[M], rho_k[M], u[3], p) and the raw EOS parameter vectors
-(``getMaterialParameters`` order, initialise.cpp:125-235: gamma, p_ref,
-e_ref, CV); the output is the final state in the AccessPattern layout.
+The reference has no adjoint. What is differentiated is its FP64 update
+(advance and the post-advance operators, main.cpp:145-187, hllc.cpp:579-707)
+over a time-step schedule frozen from a plain FP64 run at the reference
+parameters (the dt of timestep.cpp:36-70 and main.cpp:128-143): 2-D fluids
+with the stiffened-gas EOS by the dedicated reverse sweep, every other
+configuration without BVD-THINC and mixtures (solids, plasticity, 1-D, 3-D)
+by the general reverse mode. Inputs are the initial primitive fields (the
+layout ``tj_set_primitive`` takes: alpha[M], rho_k[M], u[3], p, V[9] for
+solids, epsilon[M] with plasticity) and the raw EOS parameter vectors
+(``getMaterialParameters`` order, initialise.cpp:125-235); the output is the
+final state in the AccessPattern layout. ``AdjointRun.tangent`` gives the
+forward-mode derivative of the same run along a direction.
 
     run = AdjointRun(case)
     dts = run.dt_schedule(200)
@@ -40,7 +44,7 @@ def _ptr(t: torch.Tensor) -> ctypes.c_void_p:
 
 
 class AdjointRun:
-    """An FP64 context for forward/backward passes over one 2-D domain."""
+    """An FP64 context for forward/backward and tangent passes over one domain."""
 
     def __init__(self, case: Case):
         self.case = case
