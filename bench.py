@@ -259,6 +259,7 @@ def run_gpu_arm(args):
         e2e = {"value": ncell * args.e2e_steps / (max(e2e_ms / 1e3, wall)), "unit": "cell-updates/s",
                "h2d_bytes_per_step": up_bytes, "d2h_bytes_per_step": down_bytes, "steps": args.e2e_steps,
                "path": "tj_upload_domain + tj_step + tj_download_domain (AccessPattern layout, pinned host)"}
+        e2e.update(e2e_breakdown(lib, g, host_np, up_bytes, down_bytes, max(e2e_ms, wall * 1e3) / args.e2e_steps))
 
     # accuracy and the FP64 speeds: the whole 2000-step workload (not part of
     # the timed region) in the three precisions, each timed on its own stream
@@ -486,6 +487,40 @@ def run_reference_arm(args):
         "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def e2e_breakdown(lib, g, host_np, up_bytes, down_bytes, ms_per_step, reps=10):
+    """The end-to-end step's three calls timed apart (host wall clock around
+    synchronised calls), and the host<->device link's own rate, measured by
+    plain copies of page-locked buffers of the same sizes: the part of the
+    end-to-end time the link alone needs."""
+    import torch
+
+    p = host_np.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+    def timed(f):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        for _ in range(reps):
+            f()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t) / reps * 1e3
+
+    up = timed(lambda: lib.tj_upload_domain(g.h, 0, p))
+    step = timed(lambda: (lib.tj_step(g.h, ctypes.c_double(1e300)), lib.tj_synchronize(g.h)))
+    down = timed(lambda: lib.tj_download_domain(g.h, 0, p))
+    hb = torch.empty(max(up_bytes, down_bytes) // 8, dtype=torch.float64, pin_memory=True)
+    db = torch.empty_like(hb, device="cuda")
+    nu, nd = up_bytes // 8, down_bytes // 8
+    h2d = timed(lambda: db[:nu].copy_(hb[:nu], non_blocking=True))
+    d2h = timed(lambda: hb[:nd].copy_(db[:nd], non_blocking=True))
+    link_ms = h2d + d2h
+    return {"phases_ms": {"upload": round(up, 4), "step": round(step, 4), "download": round(down, 4)},
+            "link": {"h2d_gbs": round(up_bytes / h2d / 1e6, 1), "d2h_gbs": round(down_bytes / d2h / 1e6, 1),
+                     "copy_ms_per_step": round(link_ms, 4),
+                     "frac_of_step_time": round(link_ms / ms_per_step, 3),
+                     "note": "page-locked copies of the step's upload and download sizes; the part of the "
+                             "end-to-end step that the host link alone takes"}}
 
 
 def main():
