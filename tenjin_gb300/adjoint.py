@@ -278,6 +278,67 @@ def interface_problem_check(n: int = 512, nsteps: int = 200, stride: int = 20, n
             "base_background": background}
 
 
+def general_check(name: str = "copper", n: int = 24, nsteps: int = 4, stride: int = 2, ndir: int = 8,
+                  seed: int = 0) -> dict:
+    """The general reverse mode (tj_forward / tj_backward on a configuration
+    the 2-D fluid adjoint does not cover) against the tangent-linear run:
+    forward and backward times, and |<w, tangent(v, ve)> - (<grad_prim0, v>
+    + <grad_eos, ve>)| relative, over `ndir` seeded white-noise directions
+    of the primitives and the EOS parameters and a seeded gradient w on the
+    final carried words. `name`: "copper" (3-D copper plate, n^3, 5-wave
+    solver, plastic radial return, cleanUpV) or "sod" (1-D shock tube, n
+    cells)."""
+    import time
+
+    from . import cases
+    from .host import carried_components
+
+    if name == "copper":
+        c = cases.copper_plate_3d(n=n, max_grid_size=n)
+        workload = f"copper plate {n}^3, {nsteps} steps, checkpoint every {stride}"
+    else:
+        c = cases.sod_1d(ncells=n, max_grid_size=n)
+        workload = f"1-D shock tube, {n} cells, {nsteps} steps, checkpoint every {stride}"
+    run = AdjointRun(c)
+    dts = run.dt_schedule(nsteps)
+    prim0 = np.ascontiguousarray(c.domains[0].prim)
+    prim = torch.from_numpy(prim0).cuda()
+    eos = run.eos_array()
+    rng = np.random.default_rng(seed)
+    out = run.forward(prim, eos, dts, stride)
+    carried = carried_components(c)
+    w = np.zeros(run.shape_state)
+    w[carried] = rng.standard_normal((len(carried),) + run.shape_state[1:])
+    scale = np.abs(out.cpu().numpy()).reshape(out.shape[0], -1).max(axis=1)
+    w /= np.where(scale > 0, scale, 1.0)[:, None, None, None]
+    wt = torch.from_numpy(w).cuda()
+    run.backward(wt)  # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    run.forward(prim, eos, dts, stride)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    gp, ge = run.backward(wt)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    gp = gp.cpu().numpy()
+    errs = []
+    for _ in range(ndir):
+        v = rng.standard_normal(prim0.shape) * np.abs(prim0) * 1e-3
+        ve = np.zeros_like(eos)
+        for m, mat in enumerate(c.materials):
+            ve[m, :len(mat.params)] = rng.standard_normal(len(mat.params)) * np.abs(eos[m, :len(mat.params)]) * 1e-3
+        _, ds = run.tangent(prim, torch.from_numpy(v).cuda(), eos, ve, dts)
+        tl = float((w * ds.cpu().numpy()).sum())
+        ad = float((gp * v).sum() + (ge * ve).sum())
+        errs.append(abs(tl - ad) / max(abs(tl), abs(ad)))
+    run.close()
+    e = np.array(errs)
+    return {"workload": workload, "forward_s": t1 - t0, "backward_s": t2 - t1, "ratio": (t2 - t1) / (t1 - t0),
+            "tangent_check": {"directions": ndir, "max_rel_err": float(e.max()),
+                              "median_rel_err": float(np.median(e))}}
+
+
 if __name__ == "__main__":
     import argparse
     import json
@@ -293,8 +354,13 @@ if __name__ == "__main__":
     ap.add_argument("--background", type=float, default=1e-3,
                     help="relative amplitude of the smooth background of the base state (0: the configuration as "
                          "stated, with exactly uniform regions)")
+    ap.add_argument("--general", choices=["copper", "sod"], default=None,
+                    help="check the general reverse mode on this case instead (--n cells per axis)")
     a = ap.parse_args()
     from . import build
     build.build()
-    print(json.dumps(interface_problem_check(a.n, a.steps, a.stride, a.dirs, step_rho=a.step_rho,
-                                             step_eos=a.step_eos, background=a.background, tlm_dirs=a.tlm_dirs)))
+    if a.general:
+        print(json.dumps(general_check(a.general, a.n, a.steps, a.stride, a.dirs)))
+    else:
+        print(json.dumps(interface_problem_check(a.n, a.steps, a.stride, a.dirs, step_rho=a.step_rho,
+                                                 step_eos=a.step_eos, background=a.background, tlm_dirs=a.tlm_dirs)))

@@ -18,11 +18,15 @@
 // nothing is summed with atomics, and the EOS-parameter adjoints are summed
 // per parameter in a fixed order, so the gradient is deterministic.
 //
+// The update of every direction but the last of a stage is affine in the
+// accumulator and the fluxes (bilinear in the non-conservative terms) and is
+// reversed by hand.
+//
 // Cost: a local Jacobian takes as many passes as the operator has inputs
-// (about 100 for a copper cell's update), so a backward step costs 50-110
-// forward steps (1-D shock tube: 48; copper plate 24^3: 109): the general
-// reverse mode is exact and deterministic; the 2-D fluid adjoint is the fast
-// one (backward about 3 forward steps).
+// (about 100 for a copper cell's last-direction update, 34 for a copper
+// face), so a backward step costs tens of forward steps: the general reverse
+// mode is exact and deterministic; the 2-D fluid adjoint is the fast one
+// (backward about 3 forward steps).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -152,6 +156,83 @@ __global__ void __launch_bounds__(kGT) k_gen_upd_rev(DevParamsT P, Fp64Bufs fb, 
                 }
         }
 #undef TJ_PASS
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Update of a direction other than the last, reversed per cell by hand: it
+// only adds dt/dx times flux differences to the conserved words, with the
+// non-conservative terms -alpha (S*_0 - S*_1) and -(2/3) V (S*_0 - S*_1) +
+// u_row (V*_0 - V*_1) (hllc.cpp:493-523), so the accumulator's adjoint passes
+// through and the flux and stage-input adjoints are its products with dt/dx
+// and those terms' factors.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kGT) k_gen_upd_rev_lin(DevParams P, Fp64Bufs fb, const double* U,
+                                                         const double* lamOut, double* lamYin, double* lamU,
+                                                         double* lamF0, double* lamF1, int d, int first)
+{
+    const long long nt = fb.ntot, nf = fb.nftot[d];
+    const int NS = P.NS, NX = P.NX;
+    const DevDomain D = fb.doms[0];
+    const double dtdx = fb.scal->dt / D.dx[d];
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < nt; g += (long long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        split3(g - D.off, D.n[0], D.n[1], i, j, k);
+        int o[3] = {0, 0, 0};
+        o[d] = 1;
+        const long long f0 = face_index(D, d, i, j, k), f1 = face_index(D, d, i + o[0], j + o[1], k + o[2]);
+        double l0[kNX], l1[kNX];
+        for (int w = 0; w < NX; ++w) l0[w] = l1[w] = 0.0;
+        auto lo = [&](int w) { return lamOut[(long long)w * nt + g]; };
+        auto u = [&](int w) { return U[(long long)w * nt + g]; };
+        const double dS = fb.FX[(long long)P.X_SSTAR * nf + f0] - fb.FX[(long long)P.X_SSTAR * nf + f1];
+        double su = 0.0;  // adjoint of S*_0 - S*_1
+        for (int m = 0; m < P.M; ++m) {
+            const double la = lo(P.S_ALPHA + m);
+            l0[P.X_ALPHA + m] += dtdx * la;
+            l1[P.X_ALPHA + m] -= dtdx * la;
+            su -= dtdx * u(P.S_ALPHA + m) * la;
+            lamU[(long long)(P.S_ALPHA + m) * nt + g] -= dtdx * dS * la;
+            const double lr = lo(P.S_ARHO + m);
+            l0[P.X_ARHO + m] += dtdx * lr;
+            l1[P.X_ARHO + m] -= dtdx * lr;
+            if (P.plastic) {
+                const double le = lo(P.S_ARE + m);
+                l0[P.X_ARE + m] += dtdx * le;
+                l1[P.X_ARE + m] -= dtdx * le;
+            }
+        }
+        for (int r = 0; r < 3; ++r) {
+            const double lm = lo(P.S_RHOU + r);
+            l0[P.X_RHOU + r] += dtdx * lm;
+            l1[P.X_RHOU + r] -= dtdx * lm;
+        }
+        l0[P.X_E] += dtdx * lo(P.S_E);
+        l1[P.X_E] -= dtdx * lo(P.S_E);
+        if (P.solid)
+            for (int qq = 0; qq < 9; ++qq) {
+                const int row = qq / 3, col = qq % 3;
+                const double lv = lo(P.S_V + qq);
+                l0[P.X_V + qq] += dtdx * lv;
+                l1[P.X_V + qq] -= dtdx * lv;
+                su -= dtdx * (2.0 / 3.0) * u(P.S_V + qq) * lv;
+                lamU[(long long)(P.S_V + qq) * nt + g] -= dtdx * (2.0 / 3.0) * dS * lv;
+                const double dV = fb.FX[(long long)(P.X_VSTAR + col) * nf + f0] - fb.FX[(long long)(P.X_VSTAR + col) * nf + f1];
+                l0[P.X_VSTAR + col] += dtdx * u(P.S_VEL + row) * lv;
+                l1[P.X_VSTAR + col] -= dtdx * u(P.S_VEL + row) * lv;
+                lamU[(long long)(P.S_VEL + row) * nt + g] += dtdx * dV * lv;
+            }
+        l0[P.X_SSTAR] += su;
+        l1[P.X_SSTAR] -= su;
+        for (int w = 0; w < NX; ++w) {
+            lamF0[(long long)w * nt + g] = l0[w];
+            lamF1[(long long)w * nt + g] = l1[w];
+        }
+        // the accumulator passes through: to U for the first direction
+        for (int w = 0; w < NS; ++w) {
+            if (first) lamU[(long long)w * nt + g] += lo(w);
+            else lamYin[(long long)w * nt + g] = lo(w);
+        }
     }
 }
 
@@ -609,8 +690,11 @@ long long gen_backward(GenAdj* a, const DevParams& P, const Fp64Bufs& b, const d
         Fp64Bufs f2 = fb;
         launches += path_dir_any(P, f2, U, a->yscr2, d, 1, 0, 0, st, nullptr);
         if (mp > 0) cudaMemsetAsync(a->geosf, 0, sizeof(double) * mp * b.nftot[d], st);
-        k_gen_upd_rev<<<gblocks(N), kGT, 0, st>>>(PT, fb, Yin, U, A0, lamOut, lamYin, lamU, lamA0, a->lamF0, a->lamF1,
-                                                  mp > 0 ? a->geos : nullptr, d, first, last, finish, npar);
+        if (!last && !finish)
+            k_gen_upd_rev_lin<<<gblocks(N), kGT, 0, st>>>(P, fb, U, lamOut, lamYin, lamU, a->lamF0, a->lamF1, d, first);
+        else
+            k_gen_upd_rev<<<gblocks(N), kGT, 0, st>>>(PT, fb, Yin, U, A0, lamOut, lamYin, lamU, lamA0, a->lamF0,
+                                                      a->lamF1, mp > 0 ? a->geos : nullptr, d, first, last, finish, npar);
         k_gen_flux_rev<<<gblocks(b.nftot[d]), kGT, 0, st>>>(PT, fb, a->lamF0, a->lamF1, a->lamLf, a->lamRf,
                                                             mp > 0 ? a->geosf : nullptr, d, npar, nfw);
         k_gen_recon_rev<<<gblocks(N), kGT, 0, st>>>(P, fb, U, a->lamLf, a->lamRf, lamU, d, nfw);
