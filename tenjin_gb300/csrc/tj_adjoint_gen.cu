@@ -567,6 +567,8 @@ void gen_destroy(GenAdj* a)
 const char* gen_unsupported(const DevParams& P, int ndom)
 {
     if (ndom != 1) return "the adjoint covers one domain";
+    if (P.NS > kNS || P.NX > kNX || P.NF > kNF || P.NCOMP > 64)
+        return "the general adjoint's per-cell arrays are smaller than this layout";
     if (P.thinc) return "the general adjoint covers MUSCL without BVD-THINC (2-D fluids with THINC: the 2-D adjoint)";
     if (P.nmix) return "the adjoint covers no mixtures";
     return nullptr;
