@@ -567,7 +567,8 @@ void gen_destroy(GenAdj* a)
 const char* gen_unsupported(const DevParams& P, int ndom)
 {
     if (ndom != 1) return "the adjoint covers one domain";
-    if (P.NS > kNS || P.NX > kNX || P.NF > kNF || P.NCOMP > 64)
+    const int nfw = 2 * P.M + 4 + (P.solid ? 9 + (P.any_solid ? 0 : 1) : 0) + (P.plastic ? P.M : 0);
+    if (P.NS > kNS || P.NX > kNX || nfw > kNF || P.NCOMP > 64)
         return "the general adjoint's per-cell arrays are smaller than this layout";
     if (P.thinc) return "the general adjoint covers MUSCL without BVD-THINC (2-D fluids with THINC: the 2-D adjoint)";
     if (P.nmix) return "the adjoint covers no mixtures";
