@@ -1157,16 +1157,16 @@ int tj_tangent(tj_ctx* c, int q, const double* prim0, const double* dprim0, cons
     const size_t pw = nprim * N, aw = (size_t)c->P.NCOMP * N;
     e = ensure_staging(c, sizeof(double) * (2 * pw + 2 * aw));
     if (e) return e;
-    double* dprim = c->staging;
-    double* dd = dprim + pw;
-    double* ap = dd + pw;
-    double* dap = ap + aw;
-    TJ_CUDA(c, cudaMemcpyAsync(dprim, prim0, sizeof(double) * pw, cudaMemcpyDefault, c->stream));
-    if (dprim0) TJ_CUDA(c, cudaMemcpyAsync(dd, dprim0, sizeof(double) * pw, cudaMemcpyDefault, c->stream));
+    double* prim_dev = c->staging;      // the primitives
+    double* dir_dev = prim_dev + pw;    // their direction
+    double* ap = dir_dev + pw;          // final values, AccessPattern layout
+    double* dap = ap + aw;              // final directions
+    TJ_CUDA(c, cudaMemcpyAsync(prim_dev, prim0, sizeof(double) * pw, cudaMemcpyDefault, c->stream));
+    if (dprim0) TJ_CUDA(c, cudaMemcpyAsync(dir_dev, dprim0, sizeof(double) * pw, cudaMemcpyDefault, c->stream));
     if (!c->tan) c->tan = tan_create();
     Fp64Bufs b = bufs(c);
-    long long n = tan_run(c->tan, c->P, b, 0, dprim, dprim0 ? dd : nullptr, deos, nsteps, dt, state ? ap : nullptr,
-                          dap, c->stream);
+    long long n = tan_run(c->tan, c->P, b, 0, prim_dev, dprim0 ? dir_dev : nullptr, deos, nsteps, dt,
+                          state ? ap : nullptr, dap, c->stream);
     if (n < 0) return fail(c, (int)n, "tj_tangent: device allocation failed");
     c->launches += n;
     if (state) TJ_CUDA(c, cudaMemcpyAsync(state, ap, sizeof(double) * aw, cudaMemcpyDefault, c->stream));
