@@ -9,9 +9,10 @@ the final carried words,
 must hold to rounding. Both differentiate the branches the FP64 run takes
 (limiter, Riemann-solver sides, the yield test, clamps), so the identity is
 exact whatever the directions -- white noise included. Cases: the 3-D copper
-plate (5-wave solver, plastic radial return, cleanUpV, Hugoniot EOS), a 2-D
-solid/fluid mixture with plasticity (Wilkins EOS), the 1-D shock tube, and
-the cylindrical and spherical radial source with reflective axes."""
+plate (5-wave solver, plastic radial return, cleanUpV, Hugoniot EOS), 2-D
+solid/fluid mixtures with plasticity (Wilkins, Romenskii and Hugoniot
+EOS), the 1-D shock tube, and the cylindrical and spherical radial source
+with reflective axes."""
 import numpy as np
 import pytest
 import torch
@@ -35,6 +36,8 @@ CASES = {
     "sod_1d": (lambda: cases.sod_1d(ncells=120, max_grid_size=60), 12, 5),
     "wilkins2d_plastic_cylindrical": (lambda: fx.build_case("wilkins2d_plastic_cylindrical"), 5, 2),
     "sod_spherical_1d": (lambda: fx.build_case("sod_spherical_1d"), 10, 4),
+    "romenskii2d_plastic": (lambda: fx.build_case("romenskii2d_plastic"), 5, 2),
+    "hugoniot2d_plastic": (lambda: fx.build_case("hugoniot2d_plastic"), 5, 2),
 }
 
 
