@@ -17,6 +17,7 @@ import numpy as np
 import pytest
 import torch
 
+import fixtures as fx
 from tenjin_gb300 import build, cases
 from tenjin_gb300.adjoint import AdjointRun
 from tenjin_gb300.host import FP64, TenjinGPU, carried_components
@@ -171,3 +172,32 @@ def test_adjoint_equals_tangent(background):
         errs.append(abs(tl - ad) / max(abs(tl), abs(ad)))
     run.close()
     assert max(errs) <= 1e-9, errs
+
+
+@pytest.mark.parametrize("name,precision,why", [
+    ("uneven3d_4dom", "fp64", "one domain"),
+    ("reactive_charge_1d", "fp64", "no mixtures"),
+    ("copper12", "mixed", "runs the FP64 path"),
+])
+def test_tangent_refuses_what_it_does_not_cover(name, precision, why):
+    from tenjin_gb300 import _lib
+    from tenjin_gb300.host import MIXED
+    c = fx.build_case(name)
+    run = AdjointRun(c)
+    if precision == "mixed":
+        run.sim.close()
+        run.sim = TenjinGPU(c, MIXED, set_initial=False)
+    prim = torch.from_numpy(np.ascontiguousarray(c.domains[0].prim[:c.nprim - c.nmix])).cuda()
+    with pytest.raises(_lib.TjError, match=why):
+        run.tangent(prim, None, run.eos_array(), None, np.full(2, 1e-9))
+    run.close()
+
+
+def test_general_adjoint_refuses_thinc():
+    from tenjin_gb300 import _lib
+    c = fx.build_case("sod_thinc_1d")
+    run = AdjointRun(c)
+    prim = torch.from_numpy(np.ascontiguousarray(c.domains[0].prim)).cuda()
+    with pytest.raises(_lib.TjError, match="BVD-THINC"):
+        run.forward(prim, run.eos_array(), np.full(2, 1e-9), 1)
+    run.close()
