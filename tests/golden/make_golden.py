@@ -38,6 +38,11 @@ FIXTURES = {
     "uneven3d_4dom": ("uneven_boxes_3d", {"nbox": 4, "lo": 6, "hi": 10, "max_steps": 8, "cfl": 0.4}),
     "fluid3d_boxes": ("fluid_boxes_3d", {"n": 12, "max_grid_size": 5, "max_steps": 5, "cfl": 0.4}),
     "copper12": ("copper_plate_3d", {"n": 12, "max_grid_size": 6, "max_steps": 8, "cfl": 0.4}),
+    # 3-D reflective walls (reflect_odd of the normal velocity along z too)
+    "copper10_reflect": ("copper_plate_3d", {"n": 10, "max_grid_size": 5, "max_steps": 6},
+                         {"lo_bc": [1, 0, 1], "hi_bc": [0, 1, 1]}),
+    "fluid3d_reflect": ("fluid_boxes_3d", {"n": 12, "max_grid_size": 5, "max_steps": 5},
+                        {"lo_bc": [1, 1, 1], "hi_bc": [1, 0, 1]}),
     "wilkins2d_plastic": ("solid_mixture_2d", {"eos": cases.EOS_WILKINS, "n": 20, "max_steps": 10}),
     "romenskii2d_plastic": ("solid_mixture_2d", {"eos": cases.EOS_ROMENSKII, "n": 20, "max_steps": 10}),
     "hugoniot2d_plastic": ("solid_mixture_2d", {"eos": cases.EOS_HUGONIOT, "n": 16, "max_steps": 10}),
