@@ -418,6 +418,37 @@ def solid_mixture_2d(eos: int = EOS_WILKINS, n: int = 20, max_steps: int = 8, se
     return c
 
 
+def solid_mixture_3d(eos: int = EOS_WILKINS, n: int = 10, max_steps: int = 6, seed: int = 1,
+                     max_grid_size: int = 5, yield_stress: float = 3e8, cfl: float = CFL_3D) -> Case:
+    """The 2-D solid/gas mixture in 3-D: solid for x < L/2 against an ideal
+    gas, a flyer region moving along x, random transverse velocities along y
+    and z and a shear perturbation of V; two materials through the 5-wave
+    solver, the Hencky closure, the radial return and cleanUpV along all
+    three directions."""
+    base = solid_mixture_2d(eos=eos, n=4, max_steps=max_steps, seed=seed, yield_stress=yield_stress)
+    c = Case(f"solid_mixture_3d_eos{eos}", 3, base.materials, solid=1, plastic=1, cfl=cfl, max_steps=max_steps)
+    prm = base.materials[0].params
+    rng = np.random.Generator(np.random.PCG64(seed))
+    prim = np.zeros((c.nprim, n, n, n))
+    x = np.arange(n)[None, None, :]
+    a = np.where(x < n // 2, 1 - 1e-6, 1e-6) * np.ones((n, n, n))
+    prim[0] = a
+    prim[1] = 1 - a
+    prim[2] = prm[4] * (1 + 0.01 * rng.standard_normal((n, n, n)))
+    prim[3] = 1.2
+    prim[4] = np.where(x < n // 3, 300.0, 0.0) * np.ones((n, n, n))
+    prim[5] = 50.0 * rng.standard_normal((n, n, n))
+    prim[6] = 50.0 * rng.standard_normal((n, n, n))
+    prim[7] = 1e5 + 1e7 * rng.uniform(size=(n, n, n))
+    V = np.eye(3)[:, :, None, None, None] + 0.01 * rng.standard_normal((3, 3, n, n, n))
+    for r in range(3):
+        for q in range(3):
+            prim[8 + 3 * r + q] = V[r, q]
+    nn = [n, n, n]
+    c.domains = [Domain(nn, [0.01, 0.01, 0.01], max_size_boxes(nn, 3, max_grid_size), prim)]
+    return c
+
+
 def fluid_boxes_3d(n: int = 12, max_grid_size: int = 5, max_steps: int = 5, seed: int = 0,
                    cfl: float = CFL_3D) -> Case:
     """One 3-D water/air domain split into several boxes (MUSCL only)."""

@@ -74,7 +74,8 @@ __device__ __noinline__ double upd_pass(const DevParamsT& P, const PathBufs<Dual
     update_cell(P, lb, X, Yw, 0LL, D, i, d, first, last, finish, dtv, FacePairLocal{F0, F1});
     const Dual* out = finish ? Aw : Yw;
     double s = 0.0;
-    for (int w = 0; w < P.NS; ++w) s += lo[w] * out[w].d;
+    for (int w = 0; w < P.NS; ++w)
+        if (lo[w] != 0.0) s += lo[w] * out[w].d;  // a zero adjoint takes no part
     return s;
 }
 
@@ -250,7 +251,8 @@ __device__ __noinline__ double flux_pass(const DevParamsT& P, const Dual* Lp, co
     for (int w = 0; w < P.NX; ++w) Fo[w] = Dual(0.0);
     store_flux(P, Fo, 1LL, 0LL, F, Ss, vstar);
     double s = 0.0;
-    for (int w = 0; w < P.NX; ++w) s += lF[w] * Fo[w].d;
+    for (int w = 0; w < P.NX; ++w)
+        if (lF[w] != 0.0) s += lF[w] * Fo[w].d;
     return s;
 }
 
@@ -439,7 +441,8 @@ __device__ __noinline__ double p2c_pass(const DevParamsT& P, const Dual* pr, Dua
     p2c(P, c);
     store_state(P, out, 1LL, 0LL, c);
     double s = 0.0;
-    for (int q = 0; q < P.NS; ++q) s += lo[q] * out[q].d;
+    for (int q = 0; q < P.NS; ++q)
+        if (lo[q] != 0.0) s += lo[q] * out[q].d;
     return s;
 }
 

@@ -616,7 +616,10 @@ __device__ inline void star_state(const PT& P, const CellT<R>& U, CellT<R>& Us, 
         Us.arho[m] = mult * U.arho[m];
         Us.rhok[m] = Us.arho[m] / Us.alpha[m];
         if (P.nmix && m == 0) Us.arl = mult * U.arl;
-        if (P.plastic && P.phase[m] == TJ_PHASE_SOLID) Us.are[m] = mult * U.are[m];
+        // a fluid carries no plastic strain: its alphaRhoEps star value is 0
+        // (the reference writes only the plastic materials' and resets the
+        // fluids' after every step, so no result depends on it)
+        if (P.plastic) Us.are[m] = P.phase[m] == TJ_PHASE_SOLID ? mult * U.are[m] : R(0.0);
         Us.rho += Us.arho[m];
     }
 #pragma unroll

@@ -43,6 +43,10 @@ FIXTURES = {
                          {"lo_bc": [1, 0, 1], "hi_bc": [0, 1, 1]}),
     "fluid3d_reflect": ("fluid_boxes_3d", {"n": 12, "max_grid_size": 5, "max_steps": 5},
                         {"lo_bc": [1, 1, 1], "hi_bc": [1, 0, 1]}),
+    # two materials (solid and gas) through the 5-wave solver in 3-D
+    "wilkins3d_plastic": ("solid_mixture_3d", {"eos": cases.EOS_WILKINS, "n": 10, "max_steps": 6}),
+    "romenskii3d_plastic_reflect": ("solid_mixture_3d", {"eos": cases.EOS_ROMENSKII, "n": 8, "max_grid_size": 4,
+                                                         "max_steps": 5}, {"lo_bc": [1, 0, 1], "hi_bc": [0, 1, 0]}),
     "wilkins2d_plastic": ("solid_mixture_2d", {"eos": cases.EOS_WILKINS, "n": 20, "max_steps": 10}),
     "romenskii2d_plastic": ("solid_mixture_2d", {"eos": cases.EOS_ROMENSKII, "n": 20, "max_steps": 10}),
     "hugoniot2d_plastic": ("solid_mixture_2d", {"eos": cases.EOS_HUGONIOT, "n": 16, "max_steps": 10}),

@@ -38,6 +38,7 @@ CASES = {
     "sod_spherical_1d": (lambda: fx.build_case("sod_spherical_1d"), 10, 4),
     "romenskii2d_plastic": (lambda: fx.build_case("romenskii2d_plastic"), 5, 2),
     "hugoniot2d_plastic": (lambda: fx.build_case("hugoniot2d_plastic"), 5, 2),
+    "romenskii3d_plastic_reflect": (lambda: fx.build_case("romenskii3d_plastic_reflect"), 4, 2),
 }
 
 

@@ -44,6 +44,14 @@ def test_copper_plate_plastic():
 
 
 @pytest.mark.parametrize("eos", [cases.EOS_WILKINS, cases.EOS_ROMENSKII, cases.EOS_HUGONIOT])
+def test_solid_fluid_mixture_3d(eos):
+    c = cases.solid_mixture_3d(eos=eos, n=12, max_grid_size=6, max_steps=8)
+    l1, dt_rel, cfg = compare(c, 8)
+    assert "binary32 per-direction" in cfg
+    assert l1 <= L1_TOL, l1
+
+
+@pytest.mark.parametrize("eos", [cases.EOS_WILKINS, cases.EOS_ROMENSKII, cases.EOS_HUGONIOT])
 def test_solid_fluid_mixture_2d(eos):
     c = cases.solid_mixture_2d(eos=eos, n=24, max_steps=10)
     l1, dt_rel, _ = compare(c, 10)
