@@ -102,3 +102,43 @@ def test_stock_libm_reference_reproduces_fixture(name):
     np.testing.assert_array_equal(r["dts"], gold["dts"])
     for q, st in enumerate(r["states"]):
         assert fx.exact_fraction(st[gold["carried"]], gold["states"][q]) == 1.0
+
+
+def _random_config(seed):
+    """A small seeded configuration with random walls and a perturbed
+    initial pressure, beyond the fixtures' settings."""
+    rng = np.random.default_rng(100 + seed)
+    walls = lambda: [int(x) for x in rng.integers(0, 2, 3)]
+    if seed == 0:
+        c = cases.solid_mixture_3d(eos=cases.EOS_ROMENSKII, n=6, max_grid_size=3, max_steps=4)
+    elif seed == 1:
+        c = cases.copper_plate_3d(n=8, max_grid_size=4, max_steps=4)
+    elif seed == 2:
+        c = cases.solid_mixture_2d(eos=cases.EOS_HUGONIOT, n=12, max_steps=6)
+        c.radial = 1
+    elif seed == 3:
+        c = cases.uneven_boxes_3d(nbox=3, lo=5, hi=9, max_steps=4, seed=int(rng.integers(1000)))
+    elif seed == 4:
+        c = cases.shock_bubble_2d(n=20, max_grid_size=7, max_steps=10, radius=0.3)
+    else:
+        c = cases.sod_1d(ncells=60, max_grid_size=17, max_steps=40)
+        c.thinc = 1
+    c.lo_bc, c.hi_bc = walls(), walls()
+    if c.radial:
+        c.lo_bc[0] = 1
+    ip = 2 * c.M + 3
+    for d in c.domains:
+        d.prim[ip] *= 1.0 + 0.02 * rng.standard_normal(d.prim[ip].shape)
+    return c
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_port_matches_live_reference_random_configs(seed):
+    c = _random_config(seed)
+    if not refio.have_ref(c.dim):
+        pytest.skip("reference binaries are built only where the reference tree exists")
+    r = refio.run_reference(c)
+    p = port.run_port(c)
+    np.testing.assert_array_equal(r["dts"], p["dts"])
+    for q in range(len(c.domains)):
+        assert fx.exact_fraction(p["states"][q], r["states"][q]) == 1.0
