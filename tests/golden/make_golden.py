@@ -43,6 +43,11 @@ FIXTURES = {
                          {"lo_bc": [1, 0, 1], "hi_bc": [0, 1, 1]}),
     "fluid3d_reflect": ("fluid_boxes_3d", {"n": 12, "max_grid_size": 5, "max_steps": 5},
                         {"lo_bc": [1, 1, 1], "hi_bc": [1, 0, 1]}),
+    # several 3-D domains with reflective walls; a small 3-D mixture with walls
+    "boxes3d_walls": ("uneven_boxes_3d", {"nbox": 3, "lo": 5, "hi": 9, "max_steps": 4},
+                      {"hi_bc": [1, 0, 1]}),
+    "mixture3d_walls": ("solid_mixture_3d", {"eos": cases.EOS_ROMENSKII, "n": 6, "max_grid_size": 3,
+                                             "max_steps": 4}, {"lo_bc": [1, 1, 0], "hi_bc": [1, 0, 0]}),
     # two materials (solid and gas) through the 5-wave solver in 3-D
     "wilkins3d_plastic": ("solid_mixture_3d", {"eos": cases.EOS_WILKINS, "n": 10, "max_steps": 6}),
     "romenskii3d_plastic_reflect": ("solid_mixture_3d", {"eos": cases.EOS_ROMENSKII, "n": 8, "max_grid_size": 4,
