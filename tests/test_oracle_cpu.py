@@ -87,7 +87,7 @@ def test_port_matches_live_reference_random_inputs():
 # reference linked against the host's own libm reproduces them bit for bit, so
 # the project-written exp/cosh/tanh/pow/log that both sides use for parity do
 # not decide these results.
-STOCK_EXACT = ["bubble32_muscl", "bubble3_tiny", "bubble4_reflect_boxes2", "copper10_reflect", "copper12",
+STOCK_EXACT = ["boxes3d_walls", "bubble32_muscl", "bubble3_tiny", "bubble4_reflect_boxes2", "copper10_reflect", "copper12",
                "fluid3d_boxes", "fluid3d_reflect", "hugoniot2d_plastic", "mixture_closed_form_2d", "sod1000_full",
                "sod200_boxes", "sod3_tiny", "sod_spherical_1d", "uneven3d_4dom", "wilkins2d_plastic_cylindrical"]
 
