@@ -85,7 +85,7 @@ def test_density_misfit_and_its_gradient():
     target = torch.rand(1, 4, 4, dtype=torch.float64)
     J = density_misfit(state, target, M, 0.25)
     rho = state[M:2 * M].sum(dim=0)
-    assert J.detach().item() == pytest.approx(0.5 * float(((rho - target) ** 2).sum()) * 0.25)
+    assert J.detach().item() == pytest.approx(0.5 * float(((rho.detach() - target) ** 2).sum()) * 0.25)
     J.backward()
     g = state.grad
     assert torch.allclose(g[M], (rho - target).detach() * 0.25) and torch.allclose(g[M + 1], g[M])
