@@ -545,7 +545,7 @@ struct GenAdj {
     double *lamF0 = nullptr, *lamF1 = nullptr, *lamLf = nullptr, *lamRf = nullptr, *geos = nullptr, *geosf = nullptr;
     double *prim0 = nullptr, *gsum = nullptr;
     int* a_to_s = nullptr;
-    size_t key = 0;  // sizes the buffers were made for
+    long long made[8] = {};  // the sizes the buffers were made for (gen_alloc)
 };
 
 GenAdj* gen_create() { return new GenAdj(); }
@@ -557,7 +557,7 @@ static void gen_free(GenAdj* a)
     a->bufs.clear();
     if (a->a_to_s) cudaFree(a->a_to_s);
     a->a_to_s = nullptr;
-    a->key = 0;
+    for (long long& m : a->made) m = 0;
 }
 
 void gen_destroy(GenAdj* a)
@@ -583,8 +583,10 @@ static int gen_alloc(GenAdj* a, const DevParams& P, const Fp64Bufs& b, int nstep
     const long long N = b.ntot;
     const int nck = (nsteps + stride - 1) / stride;
     const long long nfmax = std::max(b.nftot[0], std::max(b.nftot[1], b.nftot[2]));
-    const size_t key = (size_t)N * 1315423911u ^ (size_t)nck * 2654435761u ^ (size_t)stride * 97u ^ (size_t)P.NS * 31u;
-    if (a->key == key) return TJ_OK;
+    const long long want[8] = {N, nck, stride, P.NS, P.NX, P.NF, nfmax, (long long)P.M * 16 + P.dim};
+    bool same = true;
+    for (int k = 0; k < 8; ++k) same &= a->made[k] == want[k];
+    if (same) return TJ_OK;
     gen_free(a);
     auto al = [&](double** p, size_t n) {
         if (cudaMalloc(p, sizeof(double) * std::max<size_t>(n, 1)) != cudaSuccess) return false;
@@ -604,7 +606,7 @@ static int gen_alloc(GenAdj* a, const DevParams& P, const Fp64Bufs& b, int nstep
         gen_free(a);
         return TJ_ERR_CUDA;
     }
-    a->key = key;
+    for (int k = 0; k < 8; ++k) a->made[k] = want[k];
     return TJ_OK;
 }
 
