@@ -106,7 +106,10 @@ def test_stock_libm_reference_reproduces_fixture(name):
 
 def _random_config(seed):
     """A small seeded configuration with random walls and a perturbed
-    initial pressure, beyond the fixtures' settings."""
+    initial pressure, beyond the fixtures' settings: 3-D solid/gas mixtures,
+    the copper plate, 2-D solids with the radial source, uneven 3-D boxes,
+    THINC in 1-D and 2-D, the reactive MixtureEOS in 1-D (radial) and 2-D
+    (THINC)."""
     rng = np.random.default_rng(100 + seed)
     walls = lambda: [int(x) for x in rng.integers(0, 2, 3)]
     if seed == 0:
@@ -120,9 +123,19 @@ def _random_config(seed):
         c = cases.uneven_boxes_3d(nbox=3, lo=5, hi=9, max_steps=4, seed=int(rng.integers(1000)))
     elif seed == 4:
         c = cases.shock_bubble_2d(n=20, max_grid_size=7, max_steps=10, radius=0.3)
-    else:
+    elif seed == 5:
         c = cases.sod_1d(ncells=60, max_grid_size=17, max_steps=40)
         c.thinc = 1
+    elif seed == 6:
+        c = cases.reactive_charge(dim=2, n=16, max_grid_size=6, max_steps=8, thinc=1)
+    elif seed == 7:
+        c = cases.reactive_charge(dim=1, n=60, max_grid_size=13, max_steps=30)
+        c.radial = 1
+    elif seed == 8:
+        c = cases.solid_mixture_2d(eos=cases.EOS_ROMENSKII, n=12, max_steps=6)
+        c.radial = 1
+    else:
+        c = cases.solid_mixture_3d(eos=cases.EOS_WILKINS, n=6, max_grid_size=4, max_steps=4)
     c.lo_bc, c.hi_bc = walls(), walls()
     if c.radial:
         c.lo_bc[0] = 1
@@ -132,7 +145,7 @@ def _random_config(seed):
     return c
 
 
-@pytest.mark.parametrize("seed", range(6))
+@pytest.mark.parametrize("seed", range(10))
 def test_port_matches_live_reference_random_configs(seed):
     c = _random_config(seed)
     if not refio.have_ref(c.dim):
